@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Fused fusion-chain throughput at 640x480 (PSDF, 4 mm voxels) on one GB300.
+
+One step = one MainEngine frame of the PSDF workload (640x480, fx=fy=525,
+4 mm voxels, truncation 12 mm, 2^21 buckets): TV denoising (lambda 0.1,
+20 iterations), block allocation, frustum collection, inlier-ratio
+prediction, Bayesian update, marching cubes with low-surfel GC (recycling
+every 10th frame) and a 640x480 raycast.  Input frames are seeded synthetic
+renders of the room scene (scene.full_spline) with Gaussian noise
+sigma = 0.0012 z^2, 5 % outliers and 2 % missing pixels; the map is
+pre-fused for --prefuse frames before warm-up so the timed frames see a
+populated volume.
+
+Outputs one JSON line (rank 0):
+  value  frames/s with all input frames resident in HBM (device-to-device);
+  e2e    frames/s through the C ABI with host buffers: each frame's depth is
+         copied from pinned host memory and its raycast depth read back.
+Under torchrun each rank fuses its own replica (no collective on the data
+path); value is the aggregate over ranks with the max-over-ranks time.
+``--impl reference`` times the reference path's CPU restatement (the FP64
+oracle, all host threads) on the same workload instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "640×480 frames/s (alloc+fuse+mesh+raycast) batched vs plain, %HBM peak"
+TV_ITERS, TV_LAMBDA = 20, 0.1
+
+
+def _frame_job(args):
+    i, n_total, w, h = args
+    from meshhashing_gb300 import scene
+    wl = scene.full_spline(n_total, width=w, height=h)
+    return wl.frame(i), wl.pose(i)
+
+
+def gen_frames(indices, n_total, w=640, h=480, procs=None):
+    ctx = mp.get_context("spawn")
+    procs = procs or min(len(indices), os.cpu_count() or 4, 16)
+    with ctx.Pool(procs) as pool:
+        out = pool.map(_frame_job, [(i, n_total, w, h) for i in indices])
+    return [o[0] for o in out], [o[1] for o in out]
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.rows, self.proc, self.thread = [], None, None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if not self.rows:
+            return None
+        by_gpu = {}
+        for r in self.rows:
+            if len(r) >= 9:
+                by_gpu.setdefault(r[0], []).append(r)
+
+        def pw(rows):
+            v = [float(r[3]) for r in rows if r[3].replace(".", "", 1).isdigit()]
+            return float(np.median(v)) if v else 0.0
+        gpu = max(by_gpu, key=lambda g: pw(by_gpu[g]))
+        rows = by_gpu[gpu]
+        sm = [float(r[1]) for r in rows if r[1].isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "gpu": gpu, "samples": len(rows)}
+
+
+def workload_params():
+    from meshhashing_gb300 import config, scene
+    wl = scene.full_spline(8)
+    return config.params_for(wl, value_capacity=1 << 21, max_vertex_count=1 << 23, max_triangle_count=1 << 23,
+                             overflow_capacity=1 << 20)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def bytes_per_launch(stage, nb, px, rpx, vwork):
+    """Algorithmic bytes one launch of a stage must move."""
+    if stage == "integrate":       # sdf, inv_sigma2, a, b read+write; depth + inlier images
+        return nb * 512 * 32 + px * 8
+    if stage == "predict":         # three vertex slots per voxel, the inlier image
+        return nb * 512 * 12 + px * 4
+    if stage == "raycast":         # 2 KB sdf + 16 B entry per block in view; depth, vertex, normal out
+        return nb * (512 * 4 + 16) + rpx * 36
+    if stage == "mesh":            # 9^3 corner tile (4 fields), cube index, claim, slots; vertices out
+        return nb * (729 * 16 + 512 * (1 + 4 + 12 + 20)) + vwork * 32
+    if stage == "tv":
+        return TV_ITERS * px * 36 + px * 24
+    if stage == "alloc":
+        return px * 4
+    if stage == "collect":
+        return nb * 16 * 2
+    return 0.0
+
+
+def run_cpu_baseline(params, frames, poses, threads=None):
+    """FP64 oracle on all host threads, from an empty volume."""
+    from oracle import oracle as O
+    O.build()
+    if threads:
+        O.set_threads(threads)
+    o = O.Oracle(params, fp64=True)
+    t0 = time.perf_counter()
+    for d, T in zip(frames, poses):
+        o.frame(d, T, raycast=True, tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA)
+    dt = time.perf_counter() - t0
+    return len(frames) / dt, O.num_threads(), dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import platform
+    params = workload_params()
+    n = args.warmup + args.steps
+    frames, poses = gen_frames(list(range(n)), 500)
+    from oracle import oracle as O
+    O.build()
+    o = O.Oracle(params, fp64=True)
+    for i in range(args.warmup):
+        o.frame(frames[i], poses[i], raycast=True, tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA)
+    t0 = time.perf_counter()
+    for i in range(args.warmup, n):
+        o.frame(frames[i], poses[i], raycast=True, tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA)
+    dt = time.perf_counter() - t0
+    fps = args.steps / dt
+    cores = O.num_threads()
+    out = {"metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "impl": "reference",
+           "config": {"workload": "psdf_640x480_4mm_room_spline", "frames": f"{args.warmup}..{n - 1} from empty",
+                      "tv_iterations": TV_ITERS, "parallelism": "cpu"},
+           "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
+                            "sample": f"frames {args.warmup}..{n - 1} of the sequence, FP64 oracle, "
+                                      f"{platform.machine()}"},
+           "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--prefuse", type=int, default=40)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-frames", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    K, W, P = args.steps, args.warmup, args.prefuse
+    n_total = P + W + 2 * K
+    # frames are rendered in a spawn pool before any CUDA call
+    frames, poses = gen_frames(list(range(n_total)), max(500, n_total))
+    cpu_frames = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu_frames = (frames[:args.cpu_frames], poses[:args.cpu_frames])
+
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from meshhashing_gb300 import Volume, launch_count
+    from meshhashing_gb300 import build as B
+    B.build()
+    params = workload_params()
+    vol = Volume(params)
+    Hh, Ww = params.height, params.width
+    dev_depth = torch.from_numpy(np.stack(frames[:P + W + K])).cuda()
+    rd = torch.empty((Hh, Ww), dtype=torch.float32, device="cuda")
+    rv = torch.empty((Hh, Ww, 4), dtype=torch.float32, device="cuda")
+    rn = torch.empty((Hh, Ww, 4), dtype=torch.float32, device="cuda")
+
+    def step(i):
+        vol.integrate_frame(dev_depth[i], poses[i], on_device=True, tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA,
+                            ray_depth=rd, ray_vertex=rv, ray_normal=rn, outputs_on_device=True)
+
+    for i in range(P + W):
+        step(i)
+    torch.cuda.synchronize()
+    s0 = vol.stats()
+    vol.profile(True)
+    vol.profile_read()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler()
+    sampler.start()
+    barrier()
+    l0 = launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(P + W, P + W + K):
+        step(i)
+    e1.record()
+    barrier()
+    launches = launch_count() - l0
+    ms = e0.elapsed_time(e1)
+    clocks = sampler.stop()
+    prof = vol.profile_read()
+    vol.profile(False)
+    s1 = vol.stats()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * K / (ms / 1000.0)
+
+    # e2e: host depth in (pinned), raycast depth back to host every frame
+    host_in = [torch.from_numpy(f).pin_memory() for f in frames[P + W + K:P + W + 2 * K]]
+    host_out = torch.empty((Hh, Ww), dtype=torch.float32).pin_memory()
+    step_e2e = lambda j: vol.integrate_frame(host_in[j], poses[P + W + K + j], on_device=False,
+                                             tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA, ray_depth=host_out,
+                                             outputs_on_device=False)
+    barrier()
+    t0 = time.perf_counter()
+    for j in range(K):
+        step_e2e(j)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = world * K / e2e_s
+    s2 = vol.stats()
+
+    passes = max(s1["mesh_passes"] - s0["mesh_passes"], 1)
+    nb = (s1["candidate_sum"] - s0["candidate_sum"]) / passes
+    vwork = (s1["vertex_work_sum"] - s0["vertex_work_sum"]) / passes
+    px, rpx = Ww * Hh, params.rc_width * params.rc_height
+    peak, peak_kind = peaks()
+    stage_ms = {k: v[0] for k, v in prof.items()}
+    dom = max(("integrate", "raycast", "predict", "alloc", "collect"), key=lambda k: stage_ms[k])
+    calls = max(prof[dom][1], 1)
+    per_launch_ms = stage_ms[dom] / calls
+    alg = bytes_per_launch(dom, nb, px, rpx, vwork)
+    achieved = alg / (per_launch_ms / 1000.0) / 1e9
+    stages = {}
+    for k, (t_ms, c) in prof.items():
+        if c:
+            b = bytes_per_launch(k, nb, px, rpx, vwork)
+            gbs = b / ((t_ms / c) / 1000.0) / 1e9 if t_ms > 0 else None
+            stages[k] = {"ms_per_frame": t_ms / K, "gbs": gbs, "frac": (gbs / peak) if gbs else None}
+
+    cpu = None
+    if cpu_frames is not None:
+        fps, cores, dt = run_cpu_baseline(params, *cpu_frames)
+        cpu = {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
+               "sample": f"frames 0..{len(cpu_frames[0]) - 1} from an empty volume (FP64 oracle), {dt:.1f} s"}
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": K, "warmup": W,
+               "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f32", "data": "synthetic",
+               "config": {"workload": "psdf_640x480_4mm_room_spline", "resolution": [Ww, Hh], "voxel_mm": 4,
+                          "truncation_mm": 12, "buckets": params.bucket_count, "prefuse_frames": P,
+                          "tv_iterations": TV_ITERS, "form": "plain (per-frame stream launches)",
+                          "l2": "per-frame working set (voxel state of ~%d blocks) exceeds L2" % int(nb),
+                          "parallelism": "replicas" if world > 1 else "single"},
+               "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": px * 4 + 64,
+                       "d2h_bytes_per_step": rpx * 4},
+               "gpu_launches": int(launches),
+               "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                            "bytes_per_launch": alg},
+               "stages": stages,
+               "blocks": {"candidates_per_frame": nb, "vertices_per_frame": vwork,
+                          "allocated": s2["blocks_allocated"], "error": s2["error"]},
+               "clocks": clocks,
+               "cpu_baseline": cpu}
+        print(json.dumps(out), flush=True)
+    vol.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,234 @@
+/*
+ * meshhash.h -- C ABI of the GB300 volumetric-fusion hot path.
+ *
+ * Drop-in boundary for MeshHashing's engine entry points: the spatial hash and
+ * block pool (src/core), block allocation and the simple / Bayesian (PSDF)
+ * voxel update (src/mapping), per-block marching cubes with shared vertices
+ * (src/meshing) and the trilinear raycaster (src/visualization).
+ *
+ * Conventions
+ *  - Every entry point returns an int status (MH_OK == 0).  Device-side
+ *    failures (pool exhaustion, bounded-wait overruns) set a sticky error word
+ *    in the volume that mh_stats() reads back; no call exits the process.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *    Stage calls are asynchronous on that stream; counts stay on the device.
+ *  - Poses are row-major float 4x4: wTc maps camera to world, cTw world to
+ *    camera, as Sensor::wTc()/cTw() in sensor/rgbd_sensor.h:47-58.
+ *  - Depth is float32 metres, row-major width x height, z-depth (not range).
+ *  - Pointers marked "device" must be device memory; "host" pointers may be
+ *    pageable or pinned.  The library never frees caller memory.
+ */
+#ifndef MESHHASH_H
+#define MESHHASH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MH_OK            0
+#define MH_ERR_INVALID   1   /* bad argument or parameter */
+#define MH_ERR_CUDA      2   /* a CUDA runtime call failed */
+#define MH_ERR_CAPACITY  3   /* block / vertex / triangle / overflow pool exhausted */
+#define MH_ERR_TIMEOUT   4   /* a bounded device-side wait ran out */
+#define MH_ERR_NOMEM     5   /* device allocation failed at create time */
+#define MH_ERR_STATE     6   /* call out of order (e.g. no frame set) */
+
+/* Parameters: restates HashParams, MeshParams, VolumeParams, SensorParams,
+ * RayCasterParams and the RuntimeParams flags of core/params.h:16-99. */
+typedef struct mh_params {
+  /* HashParams (core/params.h:16-24) */
+  uint32_t bucket_count;          /* power of two */
+  uint32_t bucket_size;           /* slots per bucket; this build supports 4 */
+  uint32_t entry_count;           /* informational: bucket_count * bucket_size */
+  uint32_t linked_list_size;      /* longest overflow chain per bucket */
+  uint32_t value_capacity;        /* blocks in the pool */
+  /* MeshParams (core/params.h:26-29) */
+  uint32_t max_vertex_count;
+  uint32_t max_triangle_count;
+  /* VolumeParams (core/params.h:31-40) */
+  float    voxel_size;
+  float    truncation_distance_scale;
+  float    truncation_distance;
+  float    sdf_upper_bound;
+  uint32_t weight_sample;
+  uint32_t weight_upper_bound;    /* parsed but unused, as in the reference */
+  /* SensorParams (core/params.h:62-74) */
+  float    fx, fy, cx, cy;
+  uint32_t width, height;
+  float    min_depth_range;
+  float    max_depth_range;
+  float    range_factor;          /* used by mh_frame_set_u16 only */
+  /* RayCasterParams (core/params.h:42-58) */
+  float    rc_fx, rc_fy, rc_cx, rc_cy;
+  uint32_t rc_width, rc_height;
+  float    min_raycast_depth;
+  float    max_raycast_depth;
+  float    raycast_step;
+  float    sample_sdf_threshold;
+  float    sdf_threshold;
+  int32_t  enable_gradients;      /* raycast normals */
+  /* RuntimeParams subset (core/params.h:77-99) */
+  int32_t  enable_bayesian_update;
+  int32_t  enable_sdf_gradient;   /* vertex normals from the SDF gradient */
+  /* this build */
+  uint32_t overflow_capacity;     /* entries in the hash overflow pool */
+} mh_params;
+
+typedef struct mh_stats {
+  uint32_t error;                 /* sticky MH_ERR_* set by device code, 0 if none */
+  uint32_t blocks_allocated;      /* live blocks in the pool */
+  uint32_t block_high_water;      /* highest block index handed out + 1 */
+  uint32_t candidates;            /* entries of the current candidate list */
+  uint32_t vertices_allocated;
+  uint32_t triangles_allocated;
+  uint32_t overflow_used;         /* hash overflow entries in use */
+  uint32_t frames;                /* frames integrated by mh_integrate_frame */
+  uint32_t dropped_inserts;       /* inserts refused because a pool was full */
+  uint32_t gc_freed_blocks;       /* blocks returned by garbage collection */
+  uint32_t mesh_passes;           /* mh_mesh calls since reset */
+  uint64_t candidate_sum;         /* candidate-list lengths summed over mesh passes */
+  uint64_t vertex_work_sum;       /* vertices (re)computed, summed over mesh passes */
+} mh_stats;
+
+typedef struct mh_volume mh_volume;
+
+/* ICL-like defaults (config/ICL.yml) with a 4-slot bucket layout. */
+int mh_default_params(mh_params *p);
+
+/* HashTable / BlockArray / EntryArray / Mesh ::Resize + GeometryHelper::Init,
+ * as done by the MainEngine constructor (engine/main_engine.cc:315-336). */
+int mh_volume_create(const mh_params *p, mh_volume **out);
+/* MainEngine::~MainEngine (engine/main_engine.cc:338-344). */
+int mh_volume_destroy(mh_volume *v);
+/* MainEngine::Reset (engine/main_engine.cc:347-355). */
+int mh_volume_reset(mh_volume *v, void *stream);
+
+/* Sensor::Process + Sensor::set_transform (sensor/rgbd_sensor.cu:118-137,
+ * sensor/rgbd_sensor.h:47-50): takes float depth, marks depth outside
+ * [min_depth_range, max_depth_range] invalid as ConvertDepthFormatKernel does
+ * (sensor/preprocess.cu:25-42), resets the inlier-ratio image to 0.1
+ * (preprocess.cu:10-23) and stores wTc and cTw = inverse(wTc). */
+int mh_frame_set(mh_volume *v, const float *depth, int depth_on_device,
+                 const float wTc[16], void *stream);
+/* Same, from uint16 depth scaled by range_factor (preprocess.cu:25-42). */
+int mh_frame_set_u16(mh_volume *v, const uint16_t *depth, int depth_on_device,
+                     const float wTc[16], void *stream);
+
+/* AllocBlockArray (mapping/allocate.h:16-20, allocate.cu:101-125). */
+int mh_allocate(mh_volume *v, void *stream);
+/* CollectBlocksInFrustum (core/collect_block_array.h:26-31). */
+int mh_collect_frustum(mh_volume *v, void *stream);
+/* CollectAllBlocks (core/collect_block_array.h:16-19). */
+int mh_collect_all(mh_volume *v, void *stream);
+/* UpdateBlocksSimple (mapping/update_simple.h:21-27). */
+int mh_integrate_simple(mh_volume *v, void *stream);
+/* PredictOutlierRatio (mapping/update_bayesian.h:41-47). */
+int mh_predict_inlier(mh_volume *v, void *stream);
+/* UpdateBlocksBayesian (mapping/update_bayesian.h:33-39). */
+int mh_integrate_psdf(mh_volume *v, void *stream);
+/* MarchingCubes (meshing/marching_cubes.h:18-24): surfel pass, triangle pass
+ * and the two recycle passes over the current candidate list. */
+int mh_mesh(mh_volume *v, void *stream);
+/* CollectLowSurfelBlocks (mapping/recycle.h:40-44). */
+int mh_gc_low_surfel(mh_volume *v, void *stream);
+/* RecycleGarbageBlockArray (mapping/recycle.h:46-50). */
+int mh_gc_recycle(mh_volume *v, void *stream);
+/* StarveOccupiedBlockArray (mapping/recycle.h:18-21). */
+int mh_gc_starve(mh_volume *v, void *stream);
+/* CollectGarbageBlockArray (mapping/recycle.h:23-27). */
+int mh_gc_collect_garbage(mh_volume *v, void *stream);
+
+/* RayCaster::Cast (visualization/ray_caster.h:37-41).  Outputs (any may be
+ * NULL): depth = metric z of the hit (-inf on a miss), vertex = camera-frame
+ * point (x, y, z, 1), normal = camera-frame -grad(sdf) / |grad| (x, y, z, 1);
+ * misses are -inf.  Width x height = rc_width x rc_height. */
+int mh_raycast(mh_volume *v, const float cTw[16], float *depth, float *vertex4,
+               float *normal4, int out_on_device, void *stream);
+
+/* Primal-dual (Chambolle-Pock) TV-L2 denoising of the current depth frame, in
+ * place; invalid pixels stay invalid.  No reference counterpart: the
+ * reference's only primal-dual code is volumetric (optimize/primal_dual.h). */
+int mh_denoise_tv(mh_volume *v, float lambda, int iterations, void *stream);
+
+/* One MainEngine frame (app/reconstruction.cc:82-100): frame set, optional TV
+ * denoise (tv_iterations > 0), Mapping (main_engine.cc:100-154), Meshing
+ * (:156-174), raycast into the caller's buffers (may be NULL) and the
+ * simple-mode Recycle (:176-192).  `outputs_on_device` applies to the raycast
+ * outputs. */
+int mh_integrate_frame(mh_volume *v, const float *depth, int depth_on_device,
+                       const float wTc[16], int tv_iterations, float tv_lambda,
+                       float *ray_depth, float *ray_vertex4, float *ray_normal4,
+                       int outputs_on_device, void *stream);
+
+/* Synchronises `stream`, then reads the counters and the sticky error word. */
+int mh_stats_get(mh_volume *v, mh_stats *out, void *stream);
+/* Clears the sticky error word. */
+int mh_clear_error(mh_volume *v, void *stream);
+
+/* Host copies of state (synchronising).  Blocks are returned in pool order:
+ * pos[3n] block coordinates; sdf/weight/a/b [512n], voxel x fastest
+ * (geometry/geometry_helper.h:115-131).  Any array may be NULL.  *n_out gets
+ * the number of live blocks; at most max_blocks are written. */
+int mh_dump_blocks(mh_volume *v, int max_blocks, int32_t *pos, float *sdf,
+                   float *weight, float *a, float *b, int *n_out);
+/* Overwrite the voxel state of existing blocks (same layout as the dump);
+ * blocks not present are inserted.  Used to hand a state to the stages. */
+int mh_load_blocks(mh_volume *v, int n, const int32_t *pos, const float *sdf,
+                   const float *weight, const float *a, const float *b);
+/* Current candidate list as block coordinates pos[3n]. */
+int mh_dump_candidates(mh_volume *v, int max_n, int32_t *pos, int *n_out);
+/* Replace the candidate list by the given existing blocks. */
+int mh_set_candidates(mh_volume *v, int n, const int32_t *pos);
+/* Inlier-ratio image (width x height floats). */
+int mh_dump_inlier(mh_volume *v, float *out);
+/* Current (preprocessed) depth frame (width x height floats). */
+int mh_dump_depth(mh_volume *v, float *out);
+
+/* Mesh state in pool-independent form.  For every live vertex slot:
+ * vkeys[4i] = (voxel x, y, z, slot) of its owner, vdata[8i] = pos xyz,
+ * normal xyz, radius, ref_count (as float).  For every live triangle:
+ * tkeys[13 t] = owner cube voxel (x, y, z), triangle slot index, then its
+ * three vertices as (slot-owner voxel index into vkeys) ... see mesh.cu.
+ * Pass NULL arrays to query counts only. */
+int mh_dump_mesh(mh_volume *v, int max_vertices, int32_t *vkeys, float *vdata,
+                 int max_triangles, int32_t *tris, int *n_vertices, int *n_triangles);
+/* Per-voxel cube index of a block list (curr_cube_idx), 512 per block. */
+int mh_dump_cubes(mh_volume *v, int n, const int32_t *pos, uint8_t *cube_idx);
+/* Block bookkeeping for garbage collection: life_count_down, inner and
+ * boundary surfel counts, and the GC flag of each candidate. */
+int mh_dump_block_meta(mh_volume *v, int n, const int32_t *pos, int32_t *life,
+                       int32_t *inner, int32_t *boundary);
+int mh_dump_flags(mh_volume *v, int max_n, uint8_t *flags, int *n_out);
+
+/* Per-stage GPU time, measured with CUDA events recorded on each stage's
+ * stream around its launches (the reference's per-stage Timer and logging,
+ * util/timer.h, engine/logging_engine.cc:61-93).  Stage order: */
+#define MH_STAGE_PREPROCESS 0
+#define MH_STAGE_TV         1
+#define MH_STAGE_ALLOC      2
+#define MH_STAGE_COLLECT    3
+#define MH_STAGE_PREDICT    4
+#define MH_STAGE_INTEGRATE  5
+#define MH_STAGE_MESH       6
+#define MH_STAGE_GC         7
+#define MH_STAGE_RAYCAST    8
+#define MH_STAGE_COUNT      9
+int mh_profile_enable(mh_volume *v, int enable);
+/* Synchronises, returns the accumulated ms and call counts per stage since
+ * the last read, and resets them. */
+int mh_profile_read(mh_volume *v, double ms[MH_STAGE_COUNT], int calls[MH_STAGE_COUNT]);
+/* Number of kernels this library has launched in the process. */
+uint64_t mh_launch_count(void);
+
+/* Teschner hash of a block position (core/hash_table.h:259-269). */
+uint32_t mh_hash_bucket(int32_t x, int32_t y, int32_t z, uint32_t bucket_count);
+/* Bytes the last frame's stages needed by the algorithmic model (see the
+ * design notes); per stage: [alloc, collect, integrate, predict, mesh, raycast]. */
+int mh_bytes_model(mh_volume *v, double out[6]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MESHHASH_H */

@@ -1,0 +1,278 @@
+// mh_integrate.cu -- TSDF / PSDF voxel updates and inlier-ratio prediction.
+//
+// The reference launches one 512-thread CTA per candidate block with one
+// thread per voxel and scalar loads of a 20-byte AoS Voxel
+// (mapping/update_simple.cu:13-77, update_bayesian.cu:103-185).  Here a
+// persistent grid walks the device-resident candidate list; each 128-thread
+// CTA covers one block per iteration with 4 consecutive voxels per thread, so
+// every voxel field moves as one aligned 128-bit load/store.  Voxel fields are
+// only loaded when at least one of the thread's voxels projects onto a valid
+// depth pixel inside the truncation band.
+#include "mh_internal.cuh"
+#include "mh_kernels.h"
+
+namespace {
+
+struct VoxProj {
+  float cam_z;
+  float depth;
+  int pix;
+};
+
+// Per-voxel projection shared by the update kernels (update_simple.cu:26-46)
+__device__ __forceinline__ bool project_voxel(const DevParams &p, const float *cTw, const float *depth, int vx,
+                                              int vy, int vz, VoxProj &o) {
+  const float vs = p.voxel_size;
+  F3 c = mul_pt(cTw, f3((float)vx * vs, (float)vy * vs, (float)vz * vs));
+  const float u = c.x * p.fx / c.z + p.cx;
+  const float v = c.y * p.fy / c.z + p.cy;
+  const unsigned px = (unsigned)f2i(u + 0.5f), py = (unsigned)f2i(v + 0.5f);
+  if (px >= p.width || py >= p.height) return false;
+  const int pix = py * p.width + px;
+  const float d = __ldg(depth + pix);
+  if (depth_invalid(p, d)) return false;
+  o.cam_z = c.z;
+  o.depth = d;
+  o.pix = pix;
+  return true;
+}
+
+__device__ __forceinline__ float get(const float4 &v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
+__device__ __forceinline__ void put(float4 &v, int k, float x) {
+  if (k == 0) v.x = x;
+  else if (k == 1) v.y = x;
+  else if (k == 2) v.z = x;
+  else v.w = x;
+}
+
+}  // namespace
+
+// UpdateBlocksSimpleKernel + Voxel::Update (core/voxel.h:107-115)
+__global__ void __launch_bounds__(128) k_integrate_simple(Dev d) {
+  __shared__ float cTw[16];
+  if (threadIdx.x < 16) cTw[threadIdx.x] = d.fc->cTw[threadIdx.x];
+  __syncthreads();
+  const DevParams &p = d.p;
+  const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
+  const int t = threadIdx.x;
+  const int lx = (t & 1) * 4, ly = (t >> 1) & 7, lz = t >> 4;
+  for (int c = blockIdx.x; c < n; c += gridDim.x) {
+    const int4 cb = d.cand[c];
+    if (cb.w < 0) continue;
+    const int vx0 = cb.x * MH_BLOCK_SIDE + lx, vy = cb.y * MH_BLOCK_SIDE + ly, vz = cb.z * MH_BLOCK_SIDE + lz;
+    float sdf_new[4], w_new[4];
+    bool act[4], any = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      VoxProj o;
+      act[k] = false;
+      if (!project_voxel(p, cTw, d.depth, vx0 + k, vy, vz, o)) continue;
+      float sdf = o.depth - o.cam_z;
+      // 1 - normalized depth as (dmax - d) / (dmax - dmin): same value, no
+      // cancellation near the far limit (update_simple.cu:49-55)
+      const float far = (p.max_depth_range - o.depth) / (p.max_depth_range - p.min_depth_range);
+      const float w = fmaxf(10.0f * p.weight_sample * far, 1.0f);
+      const float tr = truncate_dist(p, o.depth);
+      if (sdf <= -tr) continue;
+      sdf = sdf >= 0.0f ? fminf(tr, sdf) : fmaxf(-tr, sdf);
+      sdf_new[k] = sdf;
+      w_new[k] = w;
+      act[k] = true;
+      any = true;
+    }
+    if (!any) continue;
+    const size_t base = (size_t)cb.w * MH_BLOCK_VOXELS + t * 4;
+    float4 S = *reinterpret_cast<const float4 *>(d.sdf + base);
+    float4 W = *reinterpret_cast<const float4 *>(d.w + base);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (!act[k]) continue;
+      const float s0 = get(S, k), w0 = get(W, k);
+      put(S, k, (s0 * w0 + sdf_new[k] * w_new[k]) / (w0 + w_new[k]));
+      put(W, k, w0 + w_new[k]);
+    }
+    *reinterpret_cast<float4 *>(d.sdf + base) = S;
+    *reinterpret_cast<float4 *>(d.w + base) = W;
+  }
+}
+
+// gaussian() of geometry/geometry_helper.h:30-34 (no 1/2 in the exponent)
+__device__ __forceinline__ float gaussianf(float x, float u, float s2) {
+  return 1.0f / (2.50662827463100050f * sqrtf(s2)) * expf(-((x - u) * (x - u)) / s2);
+}
+
+// UpdateBlocksBayesianKernel (mapping/update_bayesian.cu:103-185).  The
+// variance update uses C1 s^2 + C2 sigma^2 + C1 C2 (m - mu)^2, algebraically
+// equal to the reference's C1(s^2+m^2) + C2(sigma^2+mu^2) - sdf'^2 when
+// C1 + C2 = 1, but free of its single-precision cancellation.
+__global__ void __launch_bounds__(128) k_integrate_psdf(Dev d) {
+  __shared__ float cTw[16];
+  if (threadIdx.x < 16) cTw[threadIdx.x] = d.fc->cTw[threadIdx.x];
+  __syncthreads();
+  const DevParams &p = d.p;
+  const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
+  const int t = threadIdx.x;
+  const int lx = (t & 1) * 4, ly = (t >> 1) & 7, lz = t >> 4;
+  for (int c = blockIdx.x; c < n; c += gridDim.x) {
+    const int4 cb = d.cand[c];
+    if (cb.w < 0) continue;
+    const int vx0 = cb.x * MH_BLOCK_SIDE + lx, vy = cb.y * MH_BLOCK_SIDE + ly, vz = cb.z * MH_BLOCK_SIDE + lz;
+    float xs[4], rho[4], dep[4];
+    bool act[4], any = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      VoxProj o;
+      act[k] = false;
+      if (!project_voxel(p, cTw, d.depth, vx0 + k, vy, vz, o)) continue;
+      float x = o.depth - o.cam_z;
+      const float r = __ldg(d.inlier + o.pix);
+      const float tr = truncate_dist(p, o.depth);
+      if (x <= -tr) continue;
+      x = x >= 0.0f ? fminf(tr, x) : fmaxf(-tr, x);
+      xs[k] = x;
+      rho[k] = r;
+      dep[k] = o.depth;
+      act[k] = true;
+      any = true;
+    }
+    if (!any) continue;
+    const size_t base = (size_t)cb.w * MH_BLOCK_VOXELS + t * 4;
+    float4 S = *reinterpret_cast<const float4 *>(d.sdf + base);
+    float4 W = *reinterpret_cast<const float4 *>(d.w + base);
+    float4 A = *reinterpret_cast<const float4 *>(d.a + base);
+    float4 B = *reinterpret_cast<const float4 *>(d.b + base);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (!act[k]) continue;
+      const float x = xs[k], r = rho[k], dd = dep[k];
+      const float tau = (dd - 0.4f) * 0.012f + 0.019f;
+      const float w0 = get(W, k);
+      if (w0 == 0.0f) {
+        put(S, k, x);
+        put(W, k, 1.0f / (tau * tau));
+        put(A, k, r * 10.0f);
+        put(B, k, (1.0f - r) * 10.0f);
+        continue;
+      }
+      const float mu = get(S, k);
+      const float s2 = 1.0f / w0;
+      const float t2 = tau * tau;
+      const float ss2 = 1.0f / (1.0f / s2 + 1.0f / t2);
+      const float m = ss2 * (mu / s2 + x / t2);
+      float C1 = r * gaussianf(x, mu, s2 + t2);
+      float C2 = (dd < p.max_depth_range && dd >= p.min_depth_range) ? (1.0f - r) * 1.0f / (5.0f - 0.1f) : 1.0f;
+      const float sum = C1 + C2;
+      C1 /= sum;
+      C2 /= sum;
+      const float a = get(A, k), b = get(B, k);
+      const float f = C1 * (a + 1) / (a + b + 1) + C2 * a / (a + b + 1);
+      const float e = C1 * (a + 1) * (a + 2) / ((a + b + 1) * (a + b + 2)) + C2 * a * (a + 1) / ((a + b + 1) * (a + b + 2));
+      const float nsdf = C1 * m + C2 * mu;
+      const float dm = m - mu;
+      const float var = C1 * ss2 + C2 * s2 + C1 * C2 * (dm * dm);
+      put(S, k, nsdf);
+      put(W, k, 1.0f / var);
+      const float na = (e - f) / (f - e / f);
+      put(A, k, na);
+      put(B, k, na * (1.0f - f) / f);
+    }
+    *reinterpret_cast<float4 *>(d.sdf + base) = S;
+    *reinterpret_cast<float4 *>(d.w + base) = W;
+    *reinterpret_cast<float4 *>(d.a + base) = A;
+    *reinterpret_cast<float4 *>(d.b + base) = B;
+  }
+}
+
+// PredictOutlierRatioKernel (mapping/update_bayesian.cu:36-101).  The
+// per-pixel float max uses an integer atomicMax on the bit pattern, exact for
+// the positive ratios involved (all >= 0.01).  Blocks that own no vertex are
+// skipped.  The vertex normal is transformed by cTw as a point (with the
+// translation), as the reference does (update_bayesian.cu:83-86).
+__global__ void __launch_bounds__(128) k_predict_inlier(Dev d) {
+  __shared__ float cTw[16];
+  if (threadIdx.x < 16) cTw[threadIdx.x] = d.fc->cTw[threadIdx.x];
+  __syncthreads();
+  const DevParams &p = d.p;
+  const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
+  const int t = threadIdx.x;
+  const int lx = (t & 1) * 4, ly = (t >> 1) & 7, lz = t >> 4;
+  for (int c = blockIdx.x; c < n; c += gridDim.x) {
+    const int4 cb = d.cand[c];
+    if (cb.w < 0 || __ldg(d.nvtx + cb.w) <= 0) continue;
+    const size_t base = (size_t)cb.w * MH_BLOCK_VOXELS + t * 4;
+    const int4 *vs4 = reinterpret_cast<const int4 *>(d.vtx_slot + base * 3);
+    int4 q0 = vs4[0], q1 = vs4[1], q2 = vs4[2];
+    int slots[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+    bool has = false;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) has |= slots[k] > 0;
+    if (!has) continue;
+    const int vx0 = cb.x * MH_BLOCK_SIDE + lx, vy = cb.y * MH_BLOCK_SIDE + ly, vz = cb.z * MH_BLOCK_SIDE + lz;
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k) {
+      if (slots[3 * k] <= 0 && slots[3 * k + 1] <= 0 && slots[3 * k + 2] <= 0) continue;
+      VoxProj o;
+      if (!project_voxel(p, cTw, d.depth, vx0 + k, vy, vz, o)) continue;
+      const int px = o.pix % p.width, py = o.pix / p.width;
+      const float rx = ((float)px - p.cx) / p.fx, ry = ((float)py - p.cy) / p.fy;
+      const F3 pc = f3(o.depth * rx, o.depth * ry, o.depth);
+      const float vsdf = d.sdf[base + k], vw = d.w[base + k];
+      const F3 npc = normalize3(f3(-pc.x, -pc.y, -pc.z));
+#pragma unroll 1
+      for (int s = 0; s < 3; ++s) {
+        const int vp = slots[3 * k + s];
+        if (vp <= 0) continue;
+        const Vertex vt = d.vtx[vp];
+        const F3 cn = normalize3(mul_pt(cTw, f3(vt.nx, vt.ny, vt.nz)));
+        const float cos_a = dot3(npc, cn);
+        const F3 cx = mul_pt(cTw, f3(vt.px, vt.py, vt.pz));
+        const F3 vec = f3(pc.x - cx.x, pc.y - cx.y, pc.z - cx.z);
+        const float pd = dot3(vec, cn);
+        const float disk = sqrtf(dot3(vec, vec) - pd * pd);
+        const float q = pd - vsdf;
+        const float w_dist = expf(-(q * q) * vw);
+        const float w_disk = 0.5f + 0.5f / (1.0f + expf(-fabsf(disk / vt.radius)));
+        float w_ang = (cos_a - 0.1736f) / (1.0f - 0.1736f);
+        w_ang = fmaxf(w_ang, 0.1f);
+        float ir = w_disk * w_dist * w_ang;
+        ir = fmaxf(ir, 0.01f);
+        atomicMax(reinterpret_cast<int *>(d.inlier + o.pix), __float_as_int(ir));
+      }
+    }
+  }
+}
+
+// Sensor::Process tail: depth validity (ConvertDepthFormatKernel,
+// sensor/preprocess.cu:25-42) and inlier-ratio reset to 0.1 (:10-23).
+__global__ void k_preprocess(Dev d, const float *src, const uint16_t *src16, float range_factor) {
+  const int n = d.p.width * d.p.height;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float z = src16 ? range_factor * (float)src16[i] : src[i];
+    const bool ok = z >= d.p.min_depth_range && z <= d.p.max_depth_range;
+    d.depth[i] = ok ? z : -__int_as_float(0x7f800000);
+    d.inlier[i] = 0.1f;
+  }
+}
+
+static int grid_persistent(int per_sm) { return mh_sm_count() * per_sm; }
+
+int launch_integrate_simple(const Dev &d, cudaStream_t s) {
+  k_integrate_simple<<<grid_persistent(12), 128, 0, s>>>(d);
+  mh_count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+int launch_integrate_psdf(const Dev &d, cudaStream_t s) {
+  k_integrate_psdf<<<grid_persistent(12), 128, 0, s>>>(d);
+  mh_count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+int launch_predict_inlier(const Dev &d, cudaStream_t s) {
+  k_predict_inlier<<<grid_persistent(12), 128, 0, s>>>(d);
+  mh_count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+int launch_preprocess(const Dev &d, const float *src, const uint16_t *src16, float range_factor, cudaStream_t s) {
+  k_preprocess<<<grid_persistent(4), 256, 0, s>>>(d, src, src16, range_factor);
+  mh_count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}

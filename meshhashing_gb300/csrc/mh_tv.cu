@@ -1,0 +1,116 @@
+// mh_tv.cu -- primal-dual TV-L2 denoising of the input depth frame.
+//
+// No reference counterpart: the reference's only primal-dual code is a
+// volumetric Huber-TV on voxel SDFs that is never called
+// (optimize/primal_dual.cu:10-223).  This is Chambolle & Pock (2011),
+// Algorithm 1 with theta = 1, on the ROF model
+//     min_u  sum_edges |grad u| + lambda/2 * sum_valid (u - f)^2
+// with depth in millimetres (the sensor's native unit), forward differences
+// over pairs of valid pixels only (invalid pixels are holes with Neumann
+// boundaries and stay invalid), tau = sigma = 1/sqrt(8).
+//
+// One launch per iteration: each thread recomputes the dual update of its own
+// pixel and of its left and upper neighbours (the ones its divergence needs)
+// from the previous iterate, so the dual and primal steps fuse into a single
+// pass with no grid-wide barrier.  The recomputed neighbour values are
+// bit-identical to the neighbours' own, so the result does not depend on the
+// tiling.
+#include "mh_internal.cuh"
+#include "mh_kernels.h"
+
+namespace {
+
+struct TvBuf {
+  const float *f;
+  const float *u, *ub, *px, *py;
+  float *u2, *ub2, *px2, *py2;
+  int W, H;
+  float lambda;
+};
+
+__device__ __forceinline__ bool valid_at(const float *f, int i) { return f[i] > -1e30f; }
+
+// dual update at pixel (x, y) from the previous iterate
+__device__ __forceinline__ void dual_at(const TvBuf &b, int x, int y, float sigma, float &ox, float &oy) {
+  const int i = y * b.W + x;
+  const bool vi = valid_at(b.f, i);
+  float gx = 0.0f, gy = 0.0f;
+  if (vi && x + 1 < b.W && valid_at(b.f, i + 1)) gx = b.ub[i + 1] - b.ub[i];
+  if (vi && y + 1 < b.H && valid_at(b.f, i + b.W)) gy = b.ub[i + b.W] - b.ub[i];
+  const float qx = b.px[i] + sigma * gx;
+  const float qy = b.py[i] + sigma * gy;
+  const float nrm = fmaxf(1.0f, sqrtf(qx * qx + qy * qy));
+  ox = qx / nrm;
+  oy = qy / nrm;
+}
+
+}  // namespace
+
+__global__ void k_tv_init(const float *depth, float *f, float *u, float *ub, float *px, float *py, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float z = depth[i];
+    const bool ok = z > 0.0f && z < 1e30f;
+    const float v = ok ? z * 1000.0f : -__int_as_float(0x7f800000);
+    f[i] = v;
+    u[i] = v;
+    ub[i] = v;
+    px[i] = 0.0f;
+    py[i] = 0.0f;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_tv_iter(TvBuf b) {
+  const float tau = 0.35355339059327373f, sigma = 0.35355339059327373f;
+  const int n = b.W * b.H;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int x = i % b.W, y = i / b.W;
+    float pxc, pyc;
+    dual_at(b, x, y, sigma, pxc, pyc);
+    b.px2[i] = pxc;
+    b.py2[i] = pyc;
+    if (!valid_at(b.f, i)) {
+      b.u2[i] = b.f[i];
+      b.ub2[i] = b.f[i];
+      continue;
+    }
+    float pxl = 0.0f, pyu = 0.0f, dummy;
+    if (x > 0) dual_at(b, x - 1, y, sigma, pxl, dummy);
+    if (y > 0) dual_at(b, x, y - 1, sigma, dummy, pyu);
+    const float div = (pxc - pxl) + (pyc - pyu);
+    const float u0 = b.u[i];
+    const float un = (u0 + tau * div + tau * b.lambda * b.f[i]) / (1.0f + tau * b.lambda);
+    b.u2[i] = un;
+    b.ub2[i] = 2.0f * un - u0;
+  }
+}
+
+__global__ void k_tv_out(const float *f, const float *u, float *depth, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    depth[i] = valid_at(f, i) ? u[i] * 0.001f : -__int_as_float(0x7f800000);
+}
+
+// tv holds 9 planes of W*H floats: f, (u, ub, px, py) x 2
+int launch_denoise_tv(const Dev &d, float *tv, float lambda, int iterations, cudaStream_t s) {
+  const int W = d.p.width, H = d.p.height, n = W * H;
+  const int g = min((n + 255) / 256, mh_sm_count() * 8);
+  float *f = tv;
+  float *A[4] = {tv + (size_t)n, tv + 2 * (size_t)n, tv + 3 * (size_t)n, tv + 4 * (size_t)n};
+  float *B[4] = {tv + 5 * (size_t)n, tv + 6 * (size_t)n, tv + 7 * (size_t)n, tv + 8 * (size_t)n};
+  k_tv_init<<<g, 256, 0, s>>>(d.depth, f, A[0], A[1], A[2], A[3], n);
+  for (int it = 0; it < iterations; ++it) {
+    TvBuf b;
+    b.f = f;
+    b.u = A[0], b.ub = A[1], b.px = A[2], b.py = A[3];
+    b.u2 = B[0], b.ub2 = B[1], b.px2 = B[2], b.py2 = B[3];
+    b.W = W, b.H = H, b.lambda = lambda;
+    k_tv_iter<<<g, 256, 0, s>>>(b);
+    for (int k = 0; k < 4; ++k) {
+      float *t = A[k];
+      A[k] = B[k];
+      B[k] = t;
+    }
+  }
+  k_tv_out<<<g, 256, 0, s>>>(f, A[0], d.depth, n);
+  mh_count_launches(2 + iterations);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
