@@ -28,7 +28,7 @@ def psdf_workload(width=160, height=120, n=40):
 
 
 def make(wl, **over):
-    kw = dict(value_capacity=1 << 15, bucket_count=1 << 16, max_vertex_count=1 << 20, max_triangle_count=1 << 20)
+    kw = dict(value_capacity=1 << 18, bucket_count=1 << 16, max_vertex_count=1 << 20, max_triangle_count=1 << 20)
     kw.update(over)
     p = config.params_for(wl, **kw)
     return p, Volume(p)
