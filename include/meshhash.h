@@ -74,6 +74,9 @@ typedef struct mh_params {
   int32_t  enable_sdf_gradient;   /* vertex normals from the SDF gradient */
   /* this build */
   uint32_t overflow_capacity;     /* entries in the hash overflow pool */
+  uint32_t mesh_page_capacity;    /* mesh pages (per-voxel mesh units of one
+                                     block, 18.5 KB); only blocks with surface
+                                     cubes or owned vertices take one */
 } mh_params;
 
 typedef struct mh_stats {

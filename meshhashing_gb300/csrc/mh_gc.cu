@@ -99,8 +99,10 @@ __global__ void __launch_bounds__(128) k_gc_recycle_tri(Dev d) {
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
     const int ptr = d.cand[c].w;
     if (ptr < 0 || !d.flags[c]) continue;
+    const int pg = d.page_of[ptr];
+    if (pg < 0) continue;
     for (int v = threadIdx.x; v < MH_BLOCK_VOXELS * 5; v += blockDim.x) {
-      int *ts = d.tri_slot + (size_t)ptr * MH_BLOCK_VOXELS * 5 + v;
+      int *ts = d.tri_slot + (size_t)pg * MH_BLOCK_VOXELS * 5 + v;
       const int tp = *ts;
       if (tp < 0) continue;
       const int4 ot = d.tri[tp];
@@ -122,22 +124,25 @@ __global__ void __launch_bounds__(128) k_gc_recycle_vtx(Dev d) {
     const int4 cb = d.cand[c];
     if (cb.w < 0 || !d.flags[c]) continue;
     const int ptr = cb.w;
+    const int pg = d.page_of[ptr];
     if (threadIdx.x == 0) live = 0;
     __syncthreads();
     int mine = 0, freed = 0;
-    for (int v = threadIdx.x; v < MH_BLOCK_VOXELS * 3; v += blockDim.x) {
-      int *sp = d.vtx_slot + (size_t)ptr * MH_BLOCK_VOXELS * 3 + v;
-      const int vp = *sp;
-      if (vp < 0) continue;
-      if (d.vtx[vp].ref_count <= 0) {
-        float4 *v4 = reinterpret_cast<float4 *>(d.vtx + vp);
-        v4[0] = make_float4(0.f, 0.f, 0.f, 0.f);
-        v4[1] = make_float4(0.f, 0.f, 0.f, 0.f);
-        stack_push(&d.ctr->vtx_top, d.vtx_heap, vp);
-        *sp = MH_FREE_PTR;
-        ++freed;
-      } else {
-        ++mine;
+    if (pg >= 0) {
+      for (int v = threadIdx.x; v < MH_BLOCK_VOXELS * 3; v += blockDim.x) {
+        int *sp = d.vtx_slot + (size_t)pg * MH_BLOCK_VOXELS * 3 + v;
+        const int vp = *sp;
+        if (vp < 0) continue;
+        if (d.vtx[vp].ref_count <= 0) {
+          float4 *v4 = reinterpret_cast<float4 *>(d.vtx + vp);
+          v4[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+          v4[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+          stack_push(&d.ctr->vtx_top, d.vtx_heap, vp);
+          *sp = MH_FREE_PTR;
+          ++freed;
+        } else {
+          ++mine;
+        }
       }
     }
     if (freed) atomicSub(d.nvtx + ptr, freed);
@@ -153,17 +158,15 @@ __global__ void __launch_bounds__(128) k_gc_recycle_vtx(Dev d) {
       d.inner[ptr] = 0;
       d.boundary[ptr] = 0;
       d.nvtx[ptr] = 0;
+      d.wmax[ptr] = 0.0f;
       d.cand[c].w = -1;
       atomicAdd(&d.ctr->gc_freed, 1);
     }
     const size_t base = (size_t)ptr * MH_BLOCK_VOXELS;
-    for (int v = threadIdx.x; v < MH_BLOCK_VOXELS; v += blockDim.x) {
+    for (int v = threadIdx.x; v < MH_BLOCK_VOXELS; v += blockDim.x)
       d.sdf[base + v] = 0.f, d.w[base + v] = 0.f, d.a[base + v] = 0.f, d.b[base + v] = 0.f;
-      d.cube[base + v] = 0;
-      d.claim[base + v] = 0;
-      for (int s = 0; s < 3; ++s) d.vtx_slot[(base + v) * 3 + s] = MH_FREE_PTR;
-      for (int s = 0; s < 5; ++s) d.tri_slot[(base + v) * 5 + s] = MH_FREE_PTR;
-    }
+    // the page has no triangle (freed above) and no vertex left
+    if (pg >= 0) release_page_cta(d, ptr, pg);
     __syncthreads();
     if (threadIdx.x == 0) stack_push(&d.ctr->heap_top, d.heap, ptr);
   }

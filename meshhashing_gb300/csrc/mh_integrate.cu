@@ -45,6 +45,14 @@ __device__ __forceinline__ void put(float4 &v, int k, float x) {
   else v.w = x;
 }
 
+// Raise the block's weight bound (read by the mesh pass to skip blocks that
+// cannot hold a valid cube).  Positive floats order like their bit patterns.
+__device__ __forceinline__ void note_wmax(const Dev &d, int blk, float w) {
+  const unsigned act = __activemask();
+  const unsigned m = __reduce_max_sync(act, w > 0.0f ? __float_as_uint(w) : 0u);
+  if ((int)lane_id() == __ffs(act) - 1 && m) atomicMax(reinterpret_cast<unsigned *>(d.wmax + blk), m);
+}
+
 }  // namespace
 
 // UpdateBlocksSimpleKernel + Voxel::Update (core/voxel.h:107-115)
@@ -93,6 +101,7 @@ __global__ void __launch_bounds__(128) k_integrate_simple(Dev d) {
     }
     *reinterpret_cast<float4 *>(d.sdf + base) = S;
     *reinterpret_cast<float4 *>(d.w + base) = W;
+    note_wmax(d, cb.w, fmaxf(fmaxf(W.x, W.y), fmaxf(W.z, W.w)));
   }
 }
 
@@ -180,6 +189,7 @@ __global__ void __launch_bounds__(128) k_integrate_psdf(Dev d) {
     *reinterpret_cast<float4 *>(d.w + base) = W;
     *reinterpret_cast<float4 *>(d.a + base) = A;
     *reinterpret_cast<float4 *>(d.b + base) = B;
+    note_wmax(d, cb.w, fmaxf(fmaxf(W.x, W.y), fmaxf(W.z, W.w)));
   }
 }
 
@@ -199,8 +209,10 @@ __global__ void __launch_bounds__(128) k_predict_inlier(Dev d) {
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
     const int4 cb = d.cand[c];
     if (cb.w < 0 || __ldg(d.nvtx + cb.w) <= 0) continue;
+    const int pg = __ldg(d.page_of + cb.w);
+    if (pg < 0) continue;
     const size_t base = (size_t)cb.w * MH_BLOCK_VOXELS + t * 4;
-    const int4 *vs4 = reinterpret_cast<const int4 *>(d.vtx_slot + base * 3);
+    const int4 *vs4 = reinterpret_cast<const int4 *>(d.vtx_slot + ((size_t)pg * MH_BLOCK_VOXELS + t * 4) * 3);
     int4 q0 = vs4[0], q1 = vs4[1], q2 = vs4[2];
     int slots[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
     bool has = false;

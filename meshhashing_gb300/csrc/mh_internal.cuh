@@ -9,7 +9,10 @@
 //              fastest -- sdf, weight (inv_sigma2), a, b -- so one block of
 //              one field is 2 KB contiguous and 16 B aligned.
 //   meshunit : per voxel: 3 vertex slots (i32), 5 triangle slots (i32),
-//              current cube index (u8) and a vertex-claim word (u32).
+//              current cube index (u8) and a vertex-claim word (u32), held in
+//              18.5 KB mesh pages that only blocks with surface cubes or owned
+//              vertices receive (page_of[block]); blocks in free space carry
+//              voxel state only.
 //   pools    : vertices (32 B: pos, normal, radius, ref_count), triangles
 //              (16 B: three vertex indices), each with a free-index stack.
 //   counters : one small struct in device memory, so every count a launch
@@ -55,6 +58,8 @@ struct Counters {
   int vwork_count;     // vertices to (re)compute this mesh pass
   int gc_count;        // flagged blocks of the current GC pass
   int mesh_passes;     // mesh calls since reset
+  int page_top;        // free mesh pages
+  int mesh_list_count; // candidates holding a mesh page this pass
   unsigned long long cand_sum;   // sum of candidate counts over mesh calls
   unsigned long long vwork_sum;  // sum of computed vertices over mesh calls
 };
@@ -95,10 +100,16 @@ struct Dev {
   int4 *block_pos;         // x, y, z, alive
   float *sdf, *w, *a, *b;  // [cap * 512]
   int *life, *inner, *boundary, *nvtx;  // per block
-  int *vtx_slot;           // [cap * 512 * 3]
-  int *tri_slot;           // [cap * 512 * 5]
-  uint8_t *cube;           // [cap * 512]
-  uint32_t *claim;         // [cap * 512]
+  int *page_of;            // per block: mesh page or -1
+  float *wmax;             // per block: upper bound of the largest voxel weight
+  int *vtx_slot;           // [pages * 512 * 3]
+  int *tri_slot;           // [pages * 512 * 5]
+  uint8_t *cube;           // [pages * 512]
+  uint32_t *claim;         // [pages * 512]
+  int *page_heap;          // free pages
+  int *page_owner;         // per page: block index or -1
+  int *mesh_list;          // candidates holding a page (this mesh pass)
+  int page_capacity;
   Vertex *vtx;
   int *vtx_heap;
   int4 *tri;
@@ -314,6 +325,49 @@ __device__ __forceinline__ bool spatial_gradient(const Dev &d, BlockCache &bc, F
   const float vs = d.p.voxel_size;
   g = f3((sp[0] - sn[0]) / vs, (sp[1] - sn[1]) / vs, (sp[2] - sn[2]) / vs);
   return true;
+}
+
+// Mesh page of a block, allocating one on first use.  Pages are popped only
+// by the mesh cube pass and pushed only by the recycle passes.  A racing
+// allocator waits (bounded) for the winner's page.
+__device__ __forceinline__ int ensure_page(const Dev &d, int blk) {
+  int pg = *reinterpret_cast<volatile int *>(d.page_of + blk);
+  if (pg >= 0) return pg;
+  for (int it = 0; it < MH_SPIN_LIMIT; ++it) {
+    const int old = atomicCAS(d.page_of + blk, -1, -2);
+    if (old >= 0) return old;
+    if (old == -1) {
+      const int idx = atomicSub(&d.ctr->page_top, 1) - 1;
+      if (idx < 0) {
+        atomicAdd(&d.ctr->page_top, 1);
+        set_error(d, MH_ERR_CAPACITY);
+        atomicExch(d.page_of + blk, -1);
+        return -1;
+      }
+      const int p = d.page_heap[idx];
+      d.page_owner[p] = blk;
+      __threadfence();
+      atomicExch(d.page_of + blk, p);
+      return p;
+    }
+    __nanosleep(32);
+  }
+  set_error(d, MH_ERR_TIMEOUT);
+  return -1;
+}
+
+// Return a page whose slots are all free: clear its cube and claim words.
+__device__ __forceinline__ void release_page_cta(const Dev &d, int blk, int pg) {
+  for (int v = threadIdx.x; v < MH_BLOCK_VOXELS; v += blockDim.x) {
+    d.cube[(size_t)pg * MH_BLOCK_VOXELS + v] = 0;
+    d.claim[(size_t)pg * MH_BLOCK_VOXELS + v] = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    d.page_of[blk] = -1;
+    d.page_owner[pg] = -1;
+    stack_push(&d.ctr->page_top, d.page_heap, pg);
+  }
 }
 
 // launch helpers

@@ -7,7 +7,10 @@
 // vertices carry reference counts and are freed when no triangle uses them.
 //
 // GB300 structure, per mesh call:
-//   k_mc_cubes     one 512-thread CTA per candidate block (persistent grid):
+//   k_mc_cubes     one 512-thread CTA per candidate block (persistent grid);
+//                  a block with no mesh page whose weight bound is below the
+//                  MC gate (inv_sigma2 >= 1/voxel^2) has no valid cube and is
+//                  skipped after one 4-byte read;
 //                  the 9x9x9 corner tile (block + x/y/z halo) is staged in
 //                  shared memory as valid/negative bits, after 7 neighbour
 //                  lookups per block instead of 8 per cube; each cube gets its
@@ -24,7 +27,11 @@
 //                  warp-aggregated pops (TriangleExtractionKernel, :180-275).
 //   k_mc_recycle_* surplus triangle slots and unreferenced vertices return to
 //                  their pools (RecycleTrianglesKernel / RecycleVerticesKernel,
-//                  :278-321).
+//                  :278-321); a page left with no vertex and no triangle is
+//                  returned as well.
+// Mesh units live in mesh pages: a block receives one when a cube in it has
+// triangles or a cube claims a vertex it owns.  The triangle and recycle
+// passes walk only the candidates that hold a page.
 #include "mh_internal.cuh"
 #include "mh_kernels.h"
 
@@ -65,6 +72,7 @@ __device__ __forceinline__ bool claim_slot(const Dev &d, uint32_t *cw, int slot,
 __global__ void k_mc_begin(Dev d) {
   d.ctr->epoch += 1;
   d.ctr->vwork_count = 0;
+  d.ctr->mesh_list_count = 0;
 }
 __global__ void k_mc_end(Dev d) {
   d.ctr->mesh_passes += 1;
@@ -76,6 +84,7 @@ __global__ void k_mc_end(Dev d) {
 __global__ void __launch_bounds__(512) k_mc_cubes(Dev d) {
   __shared__ uint8_t tile[729];
   __shared__ int nb[8];
+  __shared__ int own_page;
   const int tid = threadIdx.x;
   const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
   const unsigned epoch = *reinterpret_cast<volatile unsigned *>(&d.ctr->epoch);
@@ -85,6 +94,8 @@ __global__ void __launch_bounds__(512) k_mc_cubes(Dev d) {
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
     const int4 cb = d.cand[c];
     if (cb.w < 0) continue;
+    // no page and no voxel that can pass the weight gate: no valid cube
+    if (d.page_of[cb.w] < 0 && d.wmax[cb.w] < lim2) continue;
     if (tid < 8) {
       const int dx = tid & 1, dy = (tid >> 1) & 1, dz = tid >> 2;
       nb[tid] = tid == 0 ? cb.w : hash_find(d, cb.x + dx, cb.y + dy, cb.z + dz);
@@ -113,23 +124,53 @@ __global__ void __launch_bounds__(512) k_mc_cubes(Dev d) {
       cube |= ((f >> 1) & 1) << k;
     }
     if (!valid) cube = 0;
-    d.cube[(size_t)cb.w * MH_BLOCK_VOXELS + tid] = (uint8_t)cube;
-    if (cube != 0 && cube != 255) {
+    const bool surf = cube != 0 && cube != 255;
+    const int any_surf = __syncthreads_or(surf);
+    if (tid == 0) own_page = any_surf ? ensure_page(d, cb.w) : d.page_of[cb.w];
+    __syncthreads();
+    const int pg = own_page;
+    if (pg >= 0) d.cube[(size_t)pg * MH_BLOCK_VOXELS + tid] = (uint8_t)cube;
+    if (surf && pg >= 0) {
 #pragma unroll 1
       for (int e = 0; e < 12; ++e) {
         if (((cube >> kEdgeEnds[e][0]) & 1) == ((cube >> kEdgeEnds[e][1]) & 1)) continue;
         const int ox = x + kOwner[e][0], oy = y + kOwner[e][1], oz = z + kOwner[e][2];
         const int optr = nb[(ox >> 3) + 2 * (oy >> 3) + 4 * (oz >> 3)];
+        const int opg = ensure_page(d, optr);
+        if (opg < 0) continue;
         const int oli = (ox & 7) + 8 * (oy & 7) + 64 * (oz & 7);
         const int slot = kOwner[e][3];
-        if (claim_slot(d, d.claim + (size_t)optr * MH_BLOCK_VOXELS + oli, slot, epoch)) {
+        if (claim_slot(d, d.claim + (size_t)opg * MH_BLOCK_VOXELS + oli, slot, epoch)) {
           const int wi = atomicAdd(&d.ctr->vwork_count, 1);
-          if (wi < d.vwork_capacity) d.vwork[wi] = make_int4(optr, oli, slot, 0);
+          if (wi < d.vwork_capacity) d.vwork[wi] = make_int4(opg, oli, slot, optr);
           else set_error(d, MH_ERR_CAPACITY);
         }
       }
     }
     __syncthreads();
+  }
+}
+
+// candidates holding a page after pass 1; the others get zero surfel counts
+__global__ void __launch_bounds__(256) k_mc_list(Dev d) {
+  const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int i = base + threadIdx.x;
+    int ptr = -1;
+    bool keep = false;
+    if (i < n) {
+      ptr = d.cand[i].w;
+      if (ptr >= 0) {
+        keep = d.page_of[ptr] >= 0;
+        if (!keep) d.inner[ptr] = d.boundary[ptr] = 0;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    int slot = 0;
+    if (lane_id() == 0 && m) slot = atomicAdd(&d.ctr->mesh_list_count, __popc(m));
+    slot = __shfl_sync(0xffffffffu, slot, 0);
+    if (keep) d.mesh_list[slot + __popc(m & lanemask_lt())] = ptr;
   }
 }
 
@@ -151,20 +192,21 @@ __global__ void __launch_bounds__(128) k_mc_vertices(Dev d) {
     }
     const int fresh = warp_pop(d, &d.ctr->vtx_top, d.vtx_heap, live && vp < 0);
     if (!live) continue;
+    const int blk = wk.w;
     if (vp < 0) {
       if (fresh < 0) continue;
       vp = fresh;
       *slotp = vp;
-      atomicAdd(d.nvtx + wk.x, 1);
+      atomicAdd(d.nvtx + blk, 1);
     }
-    const int4 bp = d.block_pos[wk.x];
+    const int4 bp = d.block_pos[blk];
     const int slot = wk.z;
     const int v0x = bp.x * MH_BLOCK_SIDE + (wk.y & 7), v0y = bp.y * MH_BLOCK_SIDE + ((wk.y >> 3) & 7),
               v0z = bp.z * MH_BLOCK_SIDE + (wk.y >> 6);
     const int v1x = v0x + (slot == 0), v1y = v0y + (slot == 1), v1z = v0z + (slot == 2);
     BlockCache bc;
     bc.init();
-    const float d0 = d.sdf[(size_t)wk.x * MH_BLOCK_VOXELS + wk.y];
+    const float d0 = d.sdf[(size_t)blk * MH_BLOCK_VOXELS + wk.y];
     const int b1x = vox2blk(v1x), b1y = vox2blk(v1y), b1z = vox2blk(v1z);
     const int p1 = bc.get(d, b1x, b1y, b1z);
     const float d1 = p1 >= 0 ? d.sdf[(size_t)p1 * MH_BLOCK_VOXELS + (v1x - b1x * 8) + 8 * (v1y - b1y * 8) +
@@ -209,22 +251,24 @@ __global__ void __launch_bounds__(128) k_mc_vertices(Dev d) {
 
 // ------------------------------------------------------------------ pass 2
 __global__ void __launch_bounds__(512) k_mc_triangles(Dev d) {
-  __shared__ int nb[8];
+  __shared__ int nbp[8];
   __shared__ int cnt[2];
   const int tid = threadIdx.x;
-  const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
+  const int n = *reinterpret_cast<volatile int *>(&d.ctr->mesh_list_count);
   const int x = tid & 7, y = (tid >> 3) & 7, z = tid >> 6;
   const bool inner = x >= 1 && y >= 1 && z >= 1 && x < 7 && y < 7 && z < 7;
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
-    const int4 cb = d.cand[c];
-    if (cb.w < 0) continue;
+    const int blk = d.mesh_list[c];
+    const int4 bp = d.block_pos[blk];
     if (tid < 8) {
       const int dx = tid & 1, dy = (tid >> 1) & 1, dz = tid >> 2;
-      nb[tid] = tid == 0 ? cb.w : hash_find(d, cb.x + dx, cb.y + dy, cb.z + dz);
+      const int q = tid == 0 ? blk : hash_find(d, bp.x + dx, bp.y + dy, bp.z + dz);
+      nbp[tid] = q >= 0 ? d.page_of[q] : -1;
     }
     if (tid < 2) cnt[tid] = 0;
     __syncthreads();
-    const size_t vi = (size_t)cb.w * MH_BLOCK_VOXELS + tid;
+    const int pg = nbp[0];
+    const size_t vi = (size_t)pg * MH_BLOCK_VOXELS + tid;
     // surfel counts (marching_cubes.cu:191-212)
     const int *vs = d.vtx_slot + vi * 3;
     const int here = (vs[0] >= 0) + (vs[1] >= 0) + (vs[2] >= 0);
@@ -249,9 +293,9 @@ __global__ void __launch_bounds__(512) k_mc_triangles(Dev d) {
       for (int q = 0; q < 3; ++q) {
         const int e = case_edge(cube, 3 * t + q);
         const int ox = x + kOwner[e][0], oy = y + kOwner[e][1], oz = z + kOwner[e][2];
-        const int optr = nb[(ox >> 3) + 2 * (oy >> 3) + 4 * (oz >> 3)];
+        const int opg = nbp[(ox >> 3) + 2 * (oy >> 3) + 4 * (oz >> 3)];
         const int oli = (ox & 7) + 8 * (oy & 7) + 64 * (oz & 7);
-        vids[q] = d.vtx_slot[((size_t)optr * MH_BLOCK_VOXELS + oli) * 3 + kOwner[e][3]];
+        vids[q] = opg >= 0 ? d.vtx_slot[((size_t)opg * MH_BLOCK_VOXELS + oli) * 3 + kOwner[e][3]] : -1;
         okv &= vids[q] >= 0;
       }
       int tp = old;
@@ -266,7 +310,7 @@ __global__ void __launch_bounds__(512) k_mc_triangles(Dev d) {
         ts[t] = tp;
       }
       if (!okv) {
-        // vertex pool ran dry earlier in this pass; keep the slot degenerate
+        // a pool ran dry earlier in this pass; keep the slot on the reserved vertex 0
         set_error(d, MH_ERR_CAPACITY);
         d.tri[tp] = make_int4(0, 0, 0, 0);
         atomicAdd(&d.vtx[0].ref_count, 3);
@@ -279,8 +323,8 @@ __global__ void __launch_bounds__(512) k_mc_triangles(Dev d) {
     }
     __syncthreads();
     if (tid == 0) {
-      d.inner[cb.w] = cnt[0];
-      d.boundary[cb.w] = cnt[1];
+      d.inner[blk] = cnt[0];
+      d.boundary[blk] = cnt[1];
     }
     __syncthreads();
   }
@@ -288,12 +332,11 @@ __global__ void __launch_bounds__(512) k_mc_triangles(Dev d) {
 
 // ------------------------------------------------------------------ recycle
 __global__ void __launch_bounds__(128) k_mc_recycle_tri(Dev d) {
-  const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
+  const int n = *reinterpret_cast<volatile int *>(&d.ctr->mesh_list_count);
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
-    const int ptr = d.cand[c].w;
-    if (ptr < 0) continue;
+    const int pg = d.page_of[d.mesh_list[c]];
     for (int v = threadIdx.x; v < MH_BLOCK_VOXELS; v += blockDim.x) {
-      const size_t vi = (size_t)ptr * MH_BLOCK_VOXELS + v;
+      const size_t vi = (size_t)pg * MH_BLOCK_VOXELS + v;
       const int cube = d.cube[vi];
       const int ntri = (cube == 0 || cube == 255) ? 0 : case_tris(cube);
       int *ts = d.tri_slot + vi * 5;
@@ -313,15 +356,22 @@ __global__ void __launch_bounds__(128) k_mc_recycle_tri(Dev d) {
 }
 
 __global__ void __launch_bounds__(128) k_mc_recycle_vtx(Dev d) {
-  const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
+  __shared__ int live;
+  const int n = *reinterpret_cast<volatile int *>(&d.ctr->mesh_list_count);
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
-    const int ptr = d.cand[c].w;
-    if (ptr < 0) continue;
-    int freed = 0;
+    const int blk = d.mesh_list[c];
+    const int pg = d.page_of[blk];
+    if (threadIdx.x == 0) live = 0;
+    __syncthreads();
+    int freed = 0, used = 0;
     for (int v = threadIdx.x; v < MH_BLOCK_VOXELS * 3; v += blockDim.x) {
-      int *sp = d.vtx_slot + (size_t)ptr * MH_BLOCK_VOXELS * 3 + v;
+      int *sp = d.vtx_slot + (size_t)pg * MH_BLOCK_VOXELS * 3 + v;
       const int vp = *sp;
-      if (vp < 0 || d.vtx[vp].ref_count != 0) continue;
+      if (vp < 0) continue;
+      if (d.vtx[vp].ref_count != 0) {
+        ++used;
+        continue;
+      }
       float4 *v4 = reinterpret_cast<float4 *>(d.vtx + vp);
       v4[0] = make_float4(0.f, 0.f, 0.f, 0.f);
       v4[1] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -329,7 +379,15 @@ __global__ void __launch_bounds__(128) k_mc_recycle_vtx(Dev d) {
       *sp = MH_FREE_PTR;
       ++freed;
     }
-    if (freed) atomicSub(d.nvtx + ptr, freed);
+    for (int v = threadIdx.x; v < MH_BLOCK_VOXELS * 5; v += blockDim.x)
+      used += d.tri_slot[(size_t)pg * MH_BLOCK_VOXELS * 5 + v] >= 0;
+    if (freed) atomicSub(d.nvtx + blk, freed);
+    if (used) atomicAdd(&live, used);
+    __syncthreads();
+    const bool empty = live == 0;
+    __syncthreads();
+    if (empty) release_page_cta(d, blk, pg);
+    __syncthreads();
   }
 }
 
@@ -337,11 +395,12 @@ int launch_mesh(const Dev &d, cudaStream_t s) {
   const int sms = mh_sm_count();
   k_mc_begin<<<1, 1, 0, s>>>(d);
   k_mc_cubes<<<sms * 2, 512, 0, s>>>(d);
+  k_mc_list<<<sms * 4, 256, 0, s>>>(d);
   k_mc_vertices<<<sms * 8, 128, 0, s>>>(d);
   k_mc_triangles<<<sms * 2, 512, 0, s>>>(d);
   k_mc_recycle_tri<<<sms * 8, 128, 0, s>>>(d);
   k_mc_recycle_vtx<<<sms * 8, 128, 0, s>>>(d);
   k_mc_end<<<1, 1, 0, s>>>(d);
-  mh_count_launches(7);
+  mh_count_launches(8);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }

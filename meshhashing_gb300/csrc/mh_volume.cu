@@ -114,6 +114,7 @@ __global__ void k_scatter_fields(Dev d, const int *ptr, int n, const float *sdf,
   if (p < 0) return;
   for (int v = threadIdx.x; v < MH_BLOCK_VOXELS; v += blockDim.x) {
     const size_t src = (size_t)blk * MH_BLOCK_VOXELS + v, dst = (size_t)p * MH_BLOCK_VOXELS + v;
+    if (v == 0) d.wmax[p] = __int_as_float(0x7f800000);
     if (sdf) d.sdf[dst] = sdf[src];
     if (w) d.w[dst] = w[src];
     if (a) d.a[dst] = a[src];
@@ -190,6 +191,7 @@ int mh_default_params(mh_params *p) {
   p->enable_bayesian_update = 1;
   p->enable_sdf_gradient = 1;
   p->overflow_capacity = 1u << 18;
+  p->mesh_page_capacity = 50000;
   return MH_OK;
 }
 
@@ -204,6 +206,7 @@ int mh_volume_reset(mh_volume *v, void *stream) {
   const mh_params &P = v->hp;
   Dev &d = v->d;
   const size_t cap = P.value_capacity, nv = cap * MH_BLOCK_VOXELS;
+  const size_t npg = (size_t)d.page_capacity, pv = npg * MH_BLOCK_VOXELS;
   MH_CUDA_TRY(cudaMemsetAsync(d.slots, 0xFF, sizeof(HSlot) * (size_t)P.bucket_count * 4, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.overflow, 0xFF, sizeof(HSlot) * (size_t)P.overflow_capacity, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.bucket_lock, 0, sizeof(int) * (size_t)P.bucket_count, s));
@@ -212,13 +215,17 @@ int mh_volume_reset(mh_volume *v, void *stream) {
   MH_CUDA_TRY(cudaMemsetAsync(d.inner, 0, sizeof(int) * cap, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.boundary, 0, sizeof(int) * cap, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.nvtx, 0, sizeof(int) * cap, s));
-  MH_CUDA_TRY(cudaMemsetAsync(d.cube, 0, nv, s));
-  MH_CUDA_TRY(cudaMemsetAsync(d.claim, 0, sizeof(uint32_t) * nv, s));
+  MH_CUDA_TRY(cudaMemsetAsync(d.wmax, 0, sizeof(float) * cap, s));
+  MH_CUDA_TRY(cudaMemsetAsync(d.page_of, 0xFF, sizeof(int) * cap, s));
+  MH_CUDA_TRY(cudaMemsetAsync(d.page_owner, 0xFF, sizeof(int) * (size_t)npg, s));
+  MH_CUDA_TRY(cudaMemsetAsync(d.cube, 0, pv, s));
+  MH_CUDA_TRY(cudaMemsetAsync(d.claim, 0, sizeof(uint32_t) * pv, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.vtx, 0, sizeof(Vertex) * (size_t)P.max_vertex_count, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.flags, 0, cap, s));
   k_fill_i32<<<grid_for(cap), 256, 0, s>>>(d.life, cap, MH_BLOCK_LIFE);
-  k_fill_i32<<<grid_for(nv * 3), 256, 0, s>>>(d.vtx_slot, nv * 3, MH_FREE_PTR);
-  k_fill_i32<<<grid_for(nv * 5), 256, 0, s>>>(d.tri_slot, nv * 5, MH_FREE_PTR);
+  k_fill_i32<<<grid_for(pv * 3), 256, 0, s>>>(d.vtx_slot, pv * 3, MH_FREE_PTR);
+  k_fill_i32<<<grid_for(pv * 5), 256, 0, s>>>(d.tri_slot, pv * 5, MH_FREE_PTR);
+  k_stack_init<<<grid_for(npg), 256, 0, s>>>(d.page_heap, (int)npg, (int)npg);
   k_fill_i32<<<grid_for((size_t)P.max_triangle_count * 4), 256, 0, s>>>(reinterpret_cast<int *>(d.tri),
                                                                        (size_t)P.max_triangle_count * 4, -1);
   k_stack_init<<<grid_for(cap), 256, 0, s>>>(d.heap, (int)cap, (int)cap);
@@ -236,6 +243,7 @@ int mh_volume_reset(mh_volume *v, void *stream) {
   c.vtx_top = (int)P.max_vertex_count - 1;
   c.tri_top = (int)P.max_triangle_count;
   c.ovf_top = (int)P.overflow_capacity;
+  c.page_top = d.page_capacity;
   c.epoch = 0;
   MH_CUDA_TRY(cudaMemcpyAsync(d.ctr, &c, sizeof(c), cudaMemcpyHostToDevice, s));
   MH_CUDA_TRY(cudaStreamSynchronize(s));
@@ -262,6 +270,7 @@ int mh_volume_create(const mh_params *p, mh_volume **out) {
       !(P.min_raycast_depth > 0.0f) || (P.max_raycast_depth - P.min_raycast_depth) / P.raycast_step > 1e6f)
     return MH_ERR_INVALID;
   if (P.linked_list_size > 1024) return MH_ERR_INVALID;
+  if (P.mesh_page_capacity == 0 || P.mesh_page_capacity > P.value_capacity) return MH_ERR_INVALID;
 
   mh_volume *v = new mh_volume();
   v->hp = P;
@@ -308,10 +317,17 @@ int mh_volume_create(const mh_params *p, mh_volume **out) {
   A(dalloc(v, &d.inner, cap));
   A(dalloc(v, &d.boundary, cap));
   A(dalloc(v, &d.nvtx, cap));
-  A(dalloc(v, &d.vtx_slot, nv * 3));
-  A(dalloc(v, &d.tri_slot, nv * 5));
-  A(dalloc(v, &d.cube, nv));
-  A(dalloc(v, &d.claim, nv));
+  d.page_capacity = (int)P.mesh_page_capacity;
+  const size_t pv = (size_t)d.page_capacity * MH_BLOCK_VOXELS;
+  A(dalloc(v, &d.page_of, cap));
+  A(dalloc(v, &d.wmax, cap));
+  A(dalloc(v, &d.mesh_list, cap));
+  A(dalloc(v, &d.page_heap, (size_t)d.page_capacity));
+  A(dalloc(v, &d.page_owner, (size_t)d.page_capacity));
+  A(dalloc(v, &d.vtx_slot, pv * 3));
+  A(dalloc(v, &d.tri_slot, pv * 5));
+  A(dalloc(v, &d.cube, pv));
+  A(dalloc(v, &d.claim, pv));
   A(dalloc(v, &d.vtx, P.max_vertex_count));
   A(dalloc(v, &d.vtx_heap, P.max_vertex_count));
   A(dalloc(v, &d.tri, P.max_triangle_count));
@@ -683,36 +699,38 @@ int mh_dump_mesh(mh_volume *v, int max_vertices, int32_t *vkeys, float *vdata, i
                  int *n_vertices, int *n_triangles) {
   CHECK_VOL(v);
   MH_CUDA_TRY(cudaDeviceSynchronize());
-  Counters c = read_counters(v);
-  const int hw = c.high_water;
-  if (hw <= 0) {
-    if (n_vertices) *n_vertices = 0;
-    if (n_triangles) *n_triangles = 0;
-    return MH_OK;
-  }
-  std::vector<int4> bp(hw);
-  MH_CUDA_TRY(cudaMemcpy(bp.data(), v->d.block_pos, sizeof(int4) * hw, cudaMemcpyDeviceToHost));
-  const size_t nv = (size_t)hw * MH_BLOCK_VOXELS;
-  std::vector<int> vs(nv * 3), ts(nv * 5);
-  MH_CUDA_TRY(cudaMemcpy(vs.data(), v->d.vtx_slot, sizeof(int) * nv * 3, cudaMemcpyDeviceToHost));
-  MH_CUDA_TRY(cudaMemcpy(ts.data(), v->d.tri_slot, sizeof(int) * nv * 5, cudaMemcpyDeviceToHost));
+  const int np = v->d.page_capacity;
+  std::vector<int> owner(np);
+  MH_CUDA_TRY(cudaMemcpy(owner.data(), v->d.page_owner, sizeof(int) * np, cudaMemcpyDeviceToHost));
+  std::vector<int> pages;
+  for (int i = 0; i < np; ++i)
+    if (owner[i] >= 0) pages.push_back(i);
+  std::vector<int4> bp(v->hp.value_capacity);
+  MH_CUDA_TRY(cudaMemcpy(bp.data(), v->d.block_pos, sizeof(int4) * bp.size(), cudaMemcpyDeviceToHost));
+  std::vector<int> vs(MH_BLOCK_VOXELS * 3), ts(MH_BLOCK_VOXELS * 5);
   std::vector<Vertex> vtx(v->hp.max_vertex_count);
   std::vector<int4> tri(v->hp.max_triangle_count);
   MH_CUDA_TRY(cudaMemcpy(vtx.data(), v->d.vtx, sizeof(Vertex) * vtx.size(), cudaMemcpyDeviceToHost));
   MH_CUDA_TRY(cudaMemcpy(tri.data(), v->d.tri, sizeof(int4) * tri.size(), cudaMemcpyDeviceToHost));
   std::unordered_map<int, int> index;
+  struct TriRec {
+    int x, y, z, t, tp;
+  };
+  std::vector<TriRec> trecs;
   int nvx = 0;
-  for (int bi = 0; bi < hw; ++bi) {
-    if (!bp[bi].w) continue;
+  for (int pg : pages) {
+    const int4 b = bp[owner[pg]];
+    MH_CUDA_TRY(cudaMemcpy(vs.data(), v->d.vtx_slot + (size_t)pg * MH_BLOCK_VOXELS * 3, sizeof(int) * vs.size(),
+                           cudaMemcpyDeviceToHost));
+    MH_CUDA_TRY(cudaMemcpy(ts.data(), v->d.tri_slot + (size_t)pg * MH_BLOCK_VOXELS * 5, sizeof(int) * ts.size(),
+                           cudaMemcpyDeviceToHost));
     for (int li = 0; li < MH_BLOCK_VOXELS; ++li) {
+      const int gx = b.x * 8 + (li & 7), gy = b.y * 8 + ((li >> 3) & 7), gz = b.z * 8 + (li >> 6);
       for (int s = 0; s < 3; ++s) {
-        const int p = vs[((size_t)bi * MH_BLOCK_VOXELS + li) * 3 + s];
+        const int p = vs[li * 3 + s];
         if (p < 0) continue;
         if (nvx < max_vertices && vkeys && vdata) {
-          vkeys[4 * nvx] = bp[bi].x * 8 + (li & 7);
-          vkeys[4 * nvx + 1] = bp[bi].y * 8 + ((li >> 3) & 7);
-          vkeys[4 * nvx + 2] = bp[bi].z * 8 + (li >> 6);
-          vkeys[4 * nvx + 3] = s;
+          vkeys[4 * nvx] = gx, vkeys[4 * nvx + 1] = gy, vkeys[4 * nvx + 2] = gz, vkeys[4 * nvx + 3] = s;
           const Vertex &x = vtx[p];
           float *o = vdata + 8 * (size_t)nvx;
           o[0] = x.px, o[1] = x.py, o[2] = x.pz, o[3] = x.nx, o[4] = x.ny, o[5] = x.nz, o[6] = x.radius;
@@ -720,28 +738,24 @@ int mh_dump_mesh(mh_volume *v, int max_vertices, int32_t *vkeys, float *vdata, i
         }
         index[p] = nvx++;
       }
+      for (int t = 0; t < 5; ++t) {
+        const int tp = ts[li * 5 + t];
+        if (tp >= 0) trecs.push_back({gx, gy, gz, t, tp});
+      }
     }
   }
   int nt = 0;
-  for (int bi = 0; bi < hw; ++bi) {
-    if (!bp[bi].w) continue;
-    for (int li = 0; li < MH_BLOCK_VOXELS; ++li) {
-      for (int t = 0; t < 5; ++t) {
-        const int tp = ts[((size_t)bi * MH_BLOCK_VOXELS + li) * 5 + t];
-        if (tp < 0) continue;
-        if (nt < max_triangles && tris) {
-          int32_t *o = tris + 7 * (size_t)nt;
-          o[0] = bp[bi].x * 8 + (li & 7), o[1] = bp[bi].y * 8 + ((li >> 3) & 7), o[2] = bp[bi].z * 8 + (li >> 6);
-          o[3] = t;
-          const int vv[3] = {tri[tp].x, tri[tp].y, tri[tp].z};
-          for (int q = 0; q < 3; ++q) {
-            auto it = index.find(vv[q]);
-            o[4 + q] = it == index.end() ? -1 : it->second;
-          }
-        }
-        ++nt;
+  for (const TriRec &r : trecs) {
+    if (nt < max_triangles && tris) {
+      int32_t *o = tris + 7 * (size_t)nt;
+      o[0] = r.x, o[1] = r.y, o[2] = r.z, o[3] = r.t;
+      const int vv[3] = {tri[r.tp].x, tri[r.tp].y, tri[r.tp].z};
+      for (int q = 0; q < 3; ++q) {
+        auto it = index.find(vv[q]);
+        o[4 + q] = it == index.end() ? -1 : it->second;
       }
     }
+    ++nt;
   }
   if (n_vertices) *n_vertices = nvx;
   if (n_triangles) *n_triangles = nt;
@@ -755,11 +769,13 @@ int mh_dump_cubes(mh_volume *v, int n, const int32_t *pos, uint8_t *cube_idx) {
   std::vector<int> ptr;
   TRY(find_ptrs(v, n, pos, ptr, false));
   for (int i = 0; i < n; ++i) {
-    if (ptr[i] < 0) {
+    int pg = -1;
+    if (ptr[i] >= 0) MH_CUDA_TRY(cudaMemcpy(&pg, v->d.page_of + ptr[i], sizeof(int), cudaMemcpyDeviceToHost));
+    if (pg < 0) {
       memset(cube_idx + (size_t)i * MH_BLOCK_VOXELS, 0, MH_BLOCK_VOXELS);
       continue;
     }
-    MH_CUDA_TRY(cudaMemcpy(cube_idx + (size_t)i * MH_BLOCK_VOXELS, v->d.cube + (size_t)ptr[i] * MH_BLOCK_VOXELS,
+    MH_CUDA_TRY(cudaMemcpy(cube_idx + (size_t)i * MH_BLOCK_VOXELS, v->d.cube + (size_t)pg * MH_BLOCK_VOXELS,
                            MH_BLOCK_VOXELS, cudaMemcpyDeviceToHost));
   }
   return MH_OK;

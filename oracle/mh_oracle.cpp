@@ -489,7 +489,8 @@ template <class R> struct Vol {
   // (update_simple.cu:26-46, update_bayesian.cu:154-177, :222-243).  The pixel
   // choice is a discrete decision and is always made in single precision, as
   // the reference makes it; the camera-space depth is computed in R.
-  bool project_voxel(const Blk<R> *b, int i, R &cam_z, unsigned &px, unsigned &py, float &dd) const {
+  bool project_voxel(const Blk<R> *b, int i, R &cam_z, unsigned &px, unsigned &py, float &dd,
+                     float *cam_z_f = nullptr) const {
     I3 vp{b->x * kB + (i % kB), b->y * kB + (i % (kB * kB)) / kB, b->z * kB + i / (kB * kB)};
     const float vsf = p.voxel_size;
     V3<float> wpf = mk((float)vp.x * vsf, (float)vp.y * vsf, (float)vp.z * vsf);
@@ -501,7 +502,16 @@ template <class R> struct Vol {
     dd = depth[(size_t)py * p.width + px];
     if (depth_invalid(dd)) return false;
     cam_z = sizeof(R) == 4 ? (R)cpf.z : cTw.pt(voxel_to_world(vp)).z;
+    if (cam_z_f) *cam_z_f = cpf.z;
     return true;
+  }
+
+  // the truncation test `sdf <= -mu` (update_simple.cu:57-58) is a discrete
+  // decision, made in single precision in both oracle modes
+  bool trunc_reject(float d, float cam_z) const {
+    float sdf = d - cam_z;
+    float tr = p.truncation_distance + p.truncation_distance_scale * d;
+    return sdf <= -tr;
   }
 
   // ---------------------------------------------------------- simple update
@@ -514,8 +524,8 @@ template <class R> struct Vol {
       for (int i = 0; i < kBV; ++i) {
         R cz;
         unsigned px, py;
-        float df;
-        if (!project_voxel(b, i, cz, px, py, df)) continue;
+        float df, czf;
+        if (!project_voxel(b, i, cz, px, py, df, &czf)) continue;
         R d = (R)df;
         R sdf = d - cz;
         // update_simple.cu:49-55: w = max(10 ws (1 - normalized depth), 1).  FP32
@@ -530,7 +540,7 @@ template <class R> struct Vol {
           w = std::max((R)10 * (R)p.weight_sample * far, (R)1);
         }
         R tr = truncate(d);
-        if (sdf <= -tr) continue;
+        if (trunc_reject(df, czf)) continue;
         sdf = sdf >= (R)0 ? std::min(tr, sdf) : std::max(-tr, sdf);
         R W = b->w[i];
         b->sdf[i] = (b->sdf[i] * W + sdf * w) / (W + w);
@@ -609,13 +619,13 @@ template <class R> struct Vol {
       for (int i = 0; i < kBV; ++i) {
         R cz;
         unsigned px, py;
-        float df;
-        if (!project_voxel(b, i, cz, px, py, df)) continue;
+        float df, czf;
+        if (!project_voxel(b, i, cz, px, py, df, &czf)) continue;
         R d = (R)df;
         R x = d - cz;
         R rho = (R)inlier[(size_t)py * p.width + px];
         R tr = truncate(d);
-        if (x <= -tr) continue;
+        if (trunc_reject(df, czf)) continue;
         x = x >= (R)0 ? std::min(tr, x) : std::max(-tr, x);
         R tau = (d - (R)0.4f) * (R)0.012f + (R)0.019f;
         if (b->w[i] == (R)0) {
@@ -875,17 +885,88 @@ template <class R> struct Vol {
 
   // ---------------------------------------------------------- raycast
   // CastKernel (visualization/ray_caster.cu:16-150) and BisectionIntersection
-  // (geometry/isosurface_intersection.h:21-55)
-  void raycast(const M4<R> &cTw_, float *odepth, float *overt, float *onorm) const {
-    M4<R> wTc_ = inverse(cTw_);
-    if (sizeof(R) == 4) {
-      M4<float> cf;
-      for (int i = 0; i < 16; ++i) cf.e[i] = (float)cTw_.e[i];
-      M4<float> wf = inverse(cf);
-      for (int i = 0; i < 16; ++i) wTc_.e[i] = (R)wf.e[i];
+  // (geometry/isosurface_intersection.h:21-55).
+  //
+  // The march is a chain of discrete decisions (sample validity, sign change,
+  // regula-falsi side), so it always runs in single precision, recording the
+  // decisions.  In FP64 mode the hit is then re-evaluated in double along the
+  // same decisions: the two bracketing samples and the regula-falsi steps use
+  // double positions and double trilinear values.
+  struct Trace {
+    bool hit = false;
+    float t0 = 0, t1 = 0;   // bracketing samples
+    uint8_t side = 0;       // bit k: iteration k moved the left end
+  };
+
+  template <class T>
+  bool spatial_t(V3<T> pos, T &sdf) const {
+    T off = (T)p.voxel_size;
+    V3<T> pc = mk(pos.x - (T)0.5 * off, pos.y - (T)0.5 * off, pos.z - (T)0.5 * off);
+    V3<T> q = pos / off;
+    V3<T> ratio = mk(q.x - std::floor(q.x), q.y - std::floor(q.y), q.z - std::floor(q.z));
+    T s = 0;
+    for (int i = 0; i < 8; ++i) {
+      int mx = (i & 4) > 0, my = (i & 2) > 0, mz = (i & 1) > 0;
+      T rx = mx ? ratio.x : (T)1 - ratio.x;
+      T ry = my ? ratio.y : (T)1 - ratio.y;
+      T rz = mz ? ratio.z : (T)1 - ratio.z;
+      V3<T> cw = mk(pc.x + (T)mx * off, pc.y + (T)my * off, pc.z + (T)mz * off);
+      auto rnd = [&](T v) { T sg = v < (T)0 ? (T)-1 : (T)1; return f2i<T>(v / off + sg * (T)0.5); };
+      I3 v{rnd(cw.x), rnd(cw.y), rnd(cw.z)};
+      int li;
+      const Blk<R> *b = block_of(v, li);
+      if (!b) return false;
+      s += (rx * ry * rz) * (T)b->sdf[li];
     }
+    sdf = s;
+    return true;
+  }
+
+  Trace march32(const M4<float> &wTcf, int x, int y) const {
+    Trace tr;
+    const float fx = p.rc_fx, fy = p.rc_fy, cx = p.rc_cx, cy = p.rc_cy;
+    V3<float> cd = normalize(mk(((float)x - cx) / fx, ((float)y - cy) / fy, 1.0f));
+    float tmin = p.min_raycast_depth / cd.z, tmax = p.max_raycast_depth / cd.z;
+    V3<float> cam = wTcf.pt(mk(0.0f, 0.0f, 0.0f));
+    V3<float> wd = normalize(wTcf.dir(cd));
+    bool have_prev = false;
+    float prev_sdf = 0, prev_t = 0;
+    for (float t = tmin; t < tmax; t += p.raycast_step) {
+      float s;
+      if (!spatial_t<float>(cam + t * wd, s)) continue;
+      if (have_prev && prev_sdf > 0.0f && s < 0.0f) {
+        float l = prev_t, r = t, ls = prev_sdf, rs = s;
+        bool found = true;
+        uint8_t side = 0;
+        for (int k = 0; k < 3; ++k) {
+          float m = l + (ls / (ls - rs)) * (r - l);
+          float ms;
+          if (!spatial_t<float>(cam + m * wd, ms)) {
+            found = false;
+            break;
+          }
+          if ((double)(ls * ms) > 0.0) {
+            l = m, ls = ms, side |= 1 << k;
+          } else {
+            r = m, rs = ms;
+          }
+        }
+        if (found && std::fabs(prev_sdf - s) < p.sample_sdf_threshold && std::fabs(s) < p.sdf_threshold) {
+          tr.hit = true, tr.t0 = prev_t, tr.t1 = t, tr.side = side;
+          return tr;
+        }
+      }
+      prev_sdf = s, prev_t = t, have_prev = true;
+    }
+    return tr;
+  }
+
+  void raycast(const M4<R> &cTw_, float *odepth, float *overt, float *onorm) const {
+    M4<float> cf;
+    for (int i = 0; i < 16; ++i) cf.e[i] = (float)cTw_.e[i];
+    const M4<float> wf = inverse(cf);
+    const M4<R> wTc_ = sizeof(R) == 4 ? M4<R>{} : inverse(cTw_);
     int W = p.rc_width, H = p.rc_height;
-    R fx = p.rc_fx, fy = p.rc_fy, cx = p.rc_cx, cy = p.rc_cy;
 #pragma omp parallel for schedule(dynamic, 2)
     for (int y = 0; y < H; ++y) {
       for (int x = 0; x < W; ++x) {
@@ -894,60 +975,49 @@ template <class R> struct Vol {
         if (odepth) odepth[pix] = NI;
         if (overt) for (int k = 0; k < 4; ++k) overt[4 * pix + k] = NI;
         if (onorm) for (int k = 0; k < 4; ++k) onorm[4 * pix + k] = NI;
-        V3<R> cd = normalize(reproject(x, y, (R)1, fx, fy, cx, cy));
-        R tmin = (R)p.min_raycast_depth / cd.z;
-        R tmax = (R)p.max_raycast_depth / cd.z;
-        V3<R> cam = wTc_.pt(mk((R)0, (R)0, (R)0));
-        V3<R> wd = normalize(wTc_.dir(cd));
-        bool have_prev = false;
-        R prev_sdf = 0, prev_t = 0;
-        R step = (R)p.raycast_step;
-        for (R t = tmin; t < tmax; t += step) {
-          V3<R> sp = cam + t * wd;
-          R s;
-          if (!spatial(sp, s)) continue;
-          if (have_prev && prev_sdf > (R)0 && s < (R)0) {
-            // regula falsi, 3 iterations
-            R l = prev_t, r = t, m = (l + r) * (R)0.5;
-            R ls = prev_sdf, rs = s;
-            bool found = true;
-            for (int k = 0; k < 3; ++k) {
-              m = l + (ls / (ls - rs)) * (r - l);
-              R ms;
-              if (!spatial(cam + m * wd, ms)) {
-                found = false;
-                break;
-              }
-              if ((double)(ls * ms) > 0.0) {
-                l = m, ls = ms;
-              } else {
-                r = m, rs = ms;
-              }
-            }
-            if (found && std::fabs(prev_sdf - s) < (R)p.sample_sdf_threshold &&
-                std::fabs(s) < (R)p.sdf_threshold) {
-              R dz = m * cd.z;
-              if (odepth) odepth[pix] = (float)dz;
-              V3<R> vc = reproject(x, y, dz, fx, fy, cx, cy);
-              if (overt) {
-                overt[4 * pix] = (float)vc.x, overt[4 * pix + 1] = (float)vc.y;
-                overt[4 * pix + 2] = (float)vc.z, overt[4 * pix + 3] = 1.0f;
-              }
-              if (p.enable_gradients && onorm) {
-                V3<R> iso = cam + m * wd;
-                V3<R> g;
-                bool ok = gradient(iso, g);
-                R len = length(g);
-                V3<R> n = (ok && len > (R)0) ? g / len : mk((R)0, (R)0, (R)0);
-                n = mk(-n.x, -n.y, -n.z);
-                V3<R> nc = cTw_.dir(n);
-                onorm[4 * pix] = (float)nc.x, onorm[4 * pix + 1] = (float)nc.y;
-                onorm[4 * pix + 2] = (float)nc.z, onorm[4 * pix + 3] = 1.0f;
-              }
-              break;
-            }
+        Trace tr = march32(wf, x, y);
+        if (!tr.hit) continue;
+        // evaluate the hit along the recorded decisions
+        M4<R> wt;
+        for (int i = 0; i < 16; ++i) wt.e[i] = sizeof(R) == 4 ? (R)wf.e[i] : wTc_.e[i];
+        const R fx = p.rc_fx, fy = p.rc_fy, cx = p.rc_cx, cy = p.rc_cy;
+        const R rx = ((R)x - cx) / fx, ry = ((R)y - cy) / fy;
+        V3<R> cd = normalize(mk(rx, ry, (R)1));
+        V3<R> cam = wt.pt(mk((R)0, (R)0, (R)0));
+        V3<R> wd = normalize(wt.dir(cd));
+        R l = tr.t0, r = tr.t1, ls, rs, m = 0;
+        if (!spatial_t<R>(cam + l * wd, ls) || !spatial_t<R>(cam + r * wd, rs)) continue;
+        bool ok = true;
+        for (int k = 0; k < 3; ++k) {
+          m = l + (ls / (ls - rs)) * (r - l);
+          R ms;
+          if (!spatial_t<R>(cam + m * wd, ms)) {
+            ok = false;
+            break;
           }
-          prev_sdf = s, prev_t = t, have_prev = true;
+          if (tr.side & (1 << k)) {
+            l = m, ls = ms;
+          } else {
+            r = m, rs = ms;
+          }
+        }
+        if (!ok) continue;
+        R dz = m * cd.z;
+        if (odepth) odepth[pix] = (float)dz;
+        if (overt) {
+          overt[4 * pix] = (float)(dz * rx), overt[4 * pix + 1] = (float)(dz * ry);
+          overt[4 * pix + 2] = (float)dz, overt[4 * pix + 3] = 1.0f;
+        }
+        if (p.enable_gradients && onorm) {
+          V3<R> iso = cam + m * wd;
+          V3<R> g;
+          bool gok = gradient(iso, g);
+          R len = length(g);
+          V3<R> n = (gok && len > (R)0) ? g / len : mk((R)0, (R)0, (R)0);
+          n = mk(-n.x, -n.y, -n.z);
+          V3<R> nc = cTw_.dir(n);
+          onorm[4 * pix] = (float)nc.x, onorm[4 * pix + 1] = (float)nc.y;
+          onorm[4 * pix + 2] = (float)nc.z, onorm[4 * pix + 3] = 1.0f;
         }
       }
     }

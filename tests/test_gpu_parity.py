@@ -235,14 +235,14 @@ def test_raycast_matches_oracle(built):
         assert np.abs(gd[hit] - od[hit]).max() <= 1e-6
         nh = hit & np.isfinite(on[..., 0])
         assert np.abs(gn[nh] - on[nh]).max() < 1e-4
+        # FP64: same discrete path (the oracle replays the single-precision
+        # decisions), values in double -- depth within 1e-4 m everywhere
         d64, _, _ = o64.raycast(cTw)
         both = hit & np.isfinite(d64)
+        assert both.sum() >= 0.999 * hit.sum()
         diff = np.abs(gd[both] - d64[both])
-        # a crossing found at a different sample (discrete) is at least one
-        # step away; everywhere else depth agrees to 1e-4 m
-        same = diff < 0.5 * p.raycast_step
-        assert same.mean() > 0.999
-        assert diff[same].max() < 1e-4, diff[same].max()
+        assert diff.max() < 1e-4, diff.max()
+        print(f"raycast vs FP64: max |ddepth| = {diff.max():.3e} m over {both.sum()} pixels")
         gt = scene.render_depth(wl.scene, wl.camera, wl.poses[i]).astype(np.float32)
         ok = hit & (gt > 0)
         assert np.median(np.abs(gd[ok] - gt[ok])) < 0.01
