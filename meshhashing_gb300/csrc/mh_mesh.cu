@@ -136,6 +136,7 @@ __global__ void __launch_bounds__(512) k_mc_cubes(Dev d) {
         if (((cube >> kEdgeEnds[e][0]) & 1) == ((cube >> kEdgeEnds[e][1]) & 1)) continue;
         const int ox = x + kOwner[e][0], oy = y + kOwner[e][1], oz = z + kOwner[e][2];
         const int optr = nb[(ox >> 3) + 2 * (oy >> 3) + 4 * (oz >> 3)];
+        if (optr < 0) continue;
         const int opg = ensure_page(d, optr);
         if (opg < 0) continue;
         const int oli = (ox & 7) + 8 * (oy & 7) + 64 * (oz & 7);
