@@ -40,7 +40,7 @@ def make_params(width, height, fx, fy, cx, cy, voxel_size, truncation, bayesian,
     p.enable_sdf_gradient = 1
     p.overflow_capacity = overflow_capacity if overflow_capacity is not None else max(bucket_count // 4, 1024)
     p.mesh_page_capacity = (mesh_page_capacity if mesh_page_capacity is not None
-                            else max(min(value_capacity, 1 << 20) // 2, 1024))
+                            else max(min(value_capacity, 1 << 20) // 2, min(value_capacity, 1024)))
     return p
 
 

@@ -114,3 +114,4 @@ int launch_denoise_tv(const Dev &d, float *tv, float lambda, int iterations, cud
   mh_count_launches(2 + iterations);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }
+

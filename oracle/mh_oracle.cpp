@@ -922,6 +922,34 @@ template <class R> struct Vol {
     return true;
   }
 
+  // FP64 sample along a single-precision path: the cell choice (the corner
+  // voxels from rounding p - v/2 and the floor of p/v, two separate discrete
+  // results in GetSpatialValue) is taken from the single-precision position
+  // p32; the fractional weights and the sum are evaluated in R at p.
+  bool spatial_hyb(V3<R> pos, V3<float> p32, R &sdf) const {
+    const float off = p.voxel_size;
+    V3<float> pc = mk(p32.x - 0.5f * off, p32.y - 0.5f * off, p32.z - 0.5f * off);
+    V3<float> q32 = p32 / off;
+    const float fl[3] = {std::floor(q32.x), std::floor(q32.y), std::floor(q32.z)};
+    const R vs = (R)p.voxel_size;
+    const R ratio[3] = {pos.x / vs - (R)fl[0], pos.y / vs - (R)fl[1], pos.z / vs - (R)fl[2]};
+    auto rnd = [&](float v) { float sg = v < 0.0f ? -1.0f : 1.0f; return f2i<float>(v / off + sg * 0.5f); };
+    R s = 0;
+    for (int i = 0; i < 8; ++i) {
+      int mx = (i & 4) > 0, my = (i & 2) > 0, mz = (i & 1) > 0;
+      R rx = mx ? ratio[0] : (R)1 - ratio[0];
+      R ry = my ? ratio[1] : (R)1 - ratio[1];
+      R rz = mz ? ratio[2] : (R)1 - ratio[2];
+      I3 v{rnd(pc.x + (float)mx * off), rnd(pc.y + (float)my * off), rnd(pc.z + (float)mz * off)};
+      int li;
+      const Blk<R> *b = block_of(v, li);
+      if (!b) return false;
+      s += (rx * ry * rz) * (R)b->sdf[li];
+    }
+    sdf = s;
+    return true;
+  }
+
   Trace march32(const M4<float> &wTcf, int x, int y) const {
     Trace tr;
     const float fx = p.rc_fx, fy = p.rc_fy, cx = p.rc_cx, cy = p.rc_cy;
@@ -961,6 +989,42 @@ template <class R> struct Vol {
     return tr;
   }
 
+  // diagnostic: the single-precision trace of one pixel and the values the
+  // replay sees (out: t0, t1, side, s32(t0), s32(t1), sR(t0), sR(t1), m per step)
+  void debug_ray(const M4<R> &cTw_, int x, int y, double *out) const {
+    M4<float> cf;
+    for (int i = 0; i < 16; ++i) cf.e[i] = (float)cTw_.e[i];
+    const M4<float> wf = inverse(cf);
+    Trace tr = march32(wf, x, y);
+    for (int k = 0; k < 16; ++k) out[k] = 0;
+    out[0] = tr.hit, out[1] = tr.t0, out[2] = tr.t1, out[3] = tr.side;
+    if (!tr.hit) return;
+    V3<float> cdf = normalize(mk(((float)x - p.rc_cx) / p.rc_fx, ((float)y - p.rc_cy) / p.rc_fy, 1.0f));
+    V3<float> camf = wf.pt(mk(0.0f, 0.0f, 0.0f));
+    V3<float> wdf = normalize(wf.dir(cdf));
+    float a, b;
+    spatial_t<float>(camf + tr.t0 * wdf, a);
+    spatial_t<float>(camf + tr.t1 * wdf, b);
+    out[4] = a, out[5] = b;
+    const M4<R> wt = inverse(cTw_);
+    V3<R> cd = normalize(mk(((R)x - (R)p.rc_cx) / (R)p.rc_fx, ((R)y - (R)p.rc_cy) / (R)p.rc_fy, (R)1));
+    V3<R> cam = wt.pt(mk((R)0, (R)0, (R)0));
+    V3<R> wd = normalize(wt.dir(cd));
+    R ls, rs;
+    spatial_t<R>(cam + (R)tr.t0 * wd, ls);
+    spatial_t<R>(cam + (R)tr.t1 * wd, rs);
+    out[6] = ls, out[7] = rs;
+    float l = tr.t0, r = tr.t1, lsf = a, rsf = b;
+    for (int k = 0; k < 3; ++k) {
+      float m = l + (lsf / (lsf - rsf)) * (r - l);
+      float ms;
+      spatial_t<float>(camf + m * wdf, ms);
+      out[8 + 2 * k] = m, out[9 + 2 * k] = ms;
+      if ((double)(lsf * ms) > 0.0) l = m, lsf = ms;
+      else r = m, rsf = ms;
+    }
+  }
+
   void raycast(const M4<R> &cTw_, float *odepth, float *overt, float *onorm) const {
     M4<float> cf;
     for (int i = 0; i < 16; ++i) cf.e[i] = (float)cTw_.e[i];
@@ -977,7 +1041,8 @@ template <class R> struct Vol {
         if (onorm) for (int k = 0; k < 4; ++k) onorm[4 * pix + k] = NI;
         Trace tr = march32(wf, x, y);
         if (!tr.hit) continue;
-        // evaluate the hit along the recorded decisions
+        // evaluate the hit along the recorded decisions: the single-precision
+        // regula falsi runs in lockstep to supply the discrete cell choices
         M4<R> wt;
         for (int i = 0; i < 16; ++i) wt.e[i] = sizeof(R) == 4 ? (R)wf.e[i] : wTc_.e[i];
         const R fx = p.rc_fx, fy = p.rc_fy, cx = p.rc_cx, cy = p.rc_cy;
@@ -985,20 +1050,34 @@ template <class R> struct Vol {
         V3<R> cd = normalize(mk(rx, ry, (R)1));
         V3<R> cam = wt.pt(mk((R)0, (R)0, (R)0));
         V3<R> wd = normalize(wt.dir(cd));
+        V3<float> cdf = normalize(mk(((float)x - p.rc_cx) / p.rc_fx, ((float)y - p.rc_cy) / p.rc_fy, 1.0f));
+        V3<float> camf = wf.pt(mk(0.0f, 0.0f, 0.0f));
+        V3<float> wdf = normalize(wf.dir(cdf));
+        float l32 = tr.t0, r32 = tr.t1, ls32, rs32;
+        spatial_t<float>(camf + l32 * wdf, ls32);
+        spatial_t<float>(camf + r32 * wdf, rs32);
         R l = tr.t0, r = tr.t1, ls, rs, m = 0;
-        if (!spatial_t<R>(cam + l * wd, ls) || !spatial_t<R>(cam + r * wd, rs)) continue;
+        if (!spatial_hyb(cam + l * wd, camf + l32 * wdf, ls) || !spatial_hyb(cam + r * wd, camf + r32 * wdf, rs))
+          continue;
         bool ok = true;
         for (int k = 0; k < 3; ++k) {
+          const float m32 = l32 + (ls32 / (ls32 - rs32)) * (r32 - l32);
           m = l + (ls / (ls - rs)) * (r - l);
+          float ms32;
           R ms;
-          if (!spatial_t<R>(cam + m * wd, ms)) {
+          spatial_t<float>(camf + m32 * wdf, ms32);
+          if (!spatial_hyb(cam + m * wd, camf + m32 * wdf, ms)) {
             ok = false;
             break;
           }
-          if (tr.side & (1 << k)) {
-            l = m, ls = ms;
+          // a value whose sign contradicts the recorded single-precision
+          // decision is within rounding of zero: the root is at m
+          const bool left = (tr.side >> k) & 1;
+          if (left != ((double)(ls * ms) > 0.0)) ms = 0;
+          if (left) {
+            l = m, ls = ms, l32 = m32, ls32 = ms32;
           } else {
-            r = m, rs = ms;
+            r = m, rs = ms, r32 = m32, rs32 = ms32;
           }
         }
         if (!ok) continue;
@@ -1450,6 +1529,15 @@ void orc_raycast(void *hp, const float *cTw, float *depth, float *vert, float *n
     decltype(vol->cTw) m;
     for (int i = 0; i < 16; ++i) m.e[i] = cTw[i];
     vol->raycast(m, depth, vert, norm);
+  });
+}
+
+void orc_debug_ray(void *hp, const float *cTw, int x, int y, double *out) {
+  OHandle *h = (OHandle *)hp;
+  DISPATCH(h, {
+    decltype(vol->cTw) m;
+    for (int i = 0; i < 16; ++i) m.e[i] = cTw[i];
+    vol->debug_ray(m, x, y, out);
   });
 }
 

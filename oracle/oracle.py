@@ -79,6 +79,7 @@ def lib():
         L.orc_frame.argtypes = [vp, f32p, f32p, C.c_int, C.c_float, f32p, f32p, f32p]
         L.orc_denoise_tv.argtypes = [vp, C.c_float, C.c_int]
         L.orc_get_depth.argtypes = [vp, f32p]
+        L.orc_debug_ray.argtypes = [vp, f32p, C.c_int, C.c_int, C.POINTER(C.c_double)]
         L.orc_num_threads.restype = C.c_int
         L.orc_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -204,6 +205,12 @@ class Oracle:
         m = f32(cTw).reshape(16)
         self.L.orc_raycast(self.h, _p(m, C.c_float), _p(d, C.c_float), _p(v, C.c_float), _p(n, C.c_float))
         return d.reshape(H, W), v.reshape(H, W, 4), n.reshape(H, W, 4)
+
+    def debug_ray(self, cTw, x, y):
+        out = (C.c_double * 16)()
+        m = f32(cTw).reshape(16)
+        self.L.orc_debug_ray(self.h, _p(m, C.c_float), int(x), int(y), out)
+        return list(out)
 
     def frame(self, depth, wTc, raycast=False, tv_iterations=0, tv_lambda=0.1):
         """One MainEngine frame (optional TV pre-filter, Mapping, Meshing,

@@ -197,7 +197,10 @@ def test_marching_cubes_topology_exact(built):
             v.marching_cubes()
             o.mesh()
             o64.mesh()
-            np.testing.assert_array_equal(v.cubes(cand), o.cubes(cand))
+            # a cube with no surface (index 0 or 255) needs no mesh page, so a
+            # block without one reports 0 for both
+            gc, oc = v.cubes(cand), o.cubes(cand)
+            np.testing.assert_array_equal(np.where(gc == 255, 0, gc), np.where(oc == 255, 0, oc))
             nv, nt, err = _mesh_compare(v, o, p, cand)
             total_tris = nt
             # FP64 vertex positions
