@@ -155,6 +155,27 @@ int mh_raycast(mh_volume *v, const float cTw[16], float *depth, float *vertex4,
  * reference's only primal-dual code is volumetric (optimize/primal_dual.h). */
 int mh_denoise_tv(mh_volume *v, float lambda, int iterations, void *stream);
 
+/* Allocation-free variant of mh_denoise_tv for callers that cannot call
+ * cudaMalloc: code whose device memory is owned by another allocator with a
+ * fixed budget (a framework's caching allocator), or latency-critical frame
+ * loops in which cudaMalloc/cudaFree would synchronise the device.  No
+ * counterpart in the reference (which has no 2-D depth denoiser).
+ *
+ * depth_in / depth_out: device pointers, width x height float32 metres
+ * (they may be the same buffer); pixels <= 0 or non-finite are invalid and
+ * come out as -inf.  The nine scratch planes live in one fixed device array of
+ * MH_TV_STATIC_MAX_PIXELS * 9 floats (about 11 MB), held by every GPU that
+ * loads the library until the process exits; images with more than
+ * MH_TV_STATIC_MAX_PIXELS pixels are rejected with MH_ERR_CAPACITY.  The
+ * first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  All calls share the array: each call initialises every plane it
+ * reads, and calls that overlap on the GPU (other streams, other threads) race
+ * on it.  Nothing is allocated or freed, on the device or the host. */
+#define MH_TV_STATIC_MAX_PIXELS (640 * 480)
+int mh_denoise_tv_static(const float *depth_in, float *depth_out, int width, int height, float lambda,
+                         int iterations, void *stream);
+
 /* One MainEngine frame (app/reconstruction.cc:82-100): frame set, optional TV
  * denoise (tv_iterations > 0), Mapping (main_engine.cc:100-154), Meshing
  * (:156-174), raycast into the caller's buffers (may be NULL) and the

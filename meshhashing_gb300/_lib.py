@@ -60,6 +60,7 @@ SIGNATURES = {
     "mh_profile_enable": (i32, [MHV, i32]),
     "mh_profile_read": (i32, [MHV, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "mh_launch_count": (C.c_uint64, []),
+    "mh_denoise_tv_static": (i32, [vp, vp, i32, i32, C.c_float, i32, vp]),
 }
 SYMBOLS = sorted(SIGNATURES)
 

@@ -115,3 +115,62 @@ int launch_denoise_tv(const Dev &d, float *tv, float lambda, int iterations, cud
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }
 
+// ------------------------------------------------------------------ no-alloc
+// TV denoising for callers that cannot allocate device memory: the nine
+// scratch planes live in a fixed file-scope device array.  See
+// mh_denoise_tv_static in include/meshhash.h.
+#include <mutex>
+
+static __device__ __align__(256) float g_tv_static_scratch[(size_t)MH_TV_STATIC_MAX_PIXELS * 9];
+
+namespace {
+std::mutex g_tv_static_mu;
+float *g_tv_static_ptr[64] = {nullptr};  // per device: address of the array above
+}  // namespace
+
+extern "C" int mh_denoise_tv_static(const float *depth_in, float *depth_out, int width, int height, float lambda,
+                                    int iterations, void *stream) {
+  if (!depth_in || !depth_out || width <= 0 || height <= 0 || iterations < 0 || !(lambda > 0.0f))
+    return MH_ERR_INVALID;
+  if ((long long)width * height > (long long)MH_TV_STATIC_MAX_PIXELS) return MH_ERR_CAPACITY;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MH_ERR_CUDA;
+  float *scratch = nullptr;
+  {
+    // first call on a device: resolve the device address of the array (host
+    // code only sees a host-side stand-in for it)
+    std::lock_guard<std::mutex> lock(g_tv_static_mu);
+    if (!g_tv_static_ptr[dev]) {
+      void *p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_tv_static_scratch) != cudaSuccess || !p) return MH_ERR_CUDA;
+      g_tv_static_ptr[dev] = static_cast<float *>(p);
+    }
+    scratch = g_tv_static_ptr[dev];
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = width * height;
+  const int g = min((n + 255) / 256, mh_sm_count() * 8);
+  float *f = scratch;
+  float *A[4] = {scratch + (size_t)n, scratch + 2 * (size_t)n, scratch + 3 * (size_t)n, scratch + 4 * (size_t)n};
+  float *B[4] = {scratch + 5 * (size_t)n, scratch + 6 * (size_t)n, scratch + 7 * (size_t)n,
+                 scratch + 8 * (size_t)n};
+  // every plane the iterations read is written here first, so no state from
+  // an earlier call leaks into this one
+  k_tv_init<<<g, 256, 0, s>>>(depth_in, f, A[0], A[1], A[2], A[3], n);
+  for (int it = 0; it < iterations; ++it) {
+    TvBuf b;
+    b.f = f;
+    b.u = A[0], b.ub = A[1], b.px = A[2], b.py = A[3];
+    b.u2 = B[0], b.ub2 = B[1], b.px2 = B[2], b.py2 = B[3];
+    b.W = width, b.H = height, b.lambda = lambda;
+    k_tv_iter<<<g, 256, 0, s>>>(b);
+    for (int k = 0; k < 4; ++k) {
+      float *t = A[k];
+      A[k] = B[k];
+      B[k] = t;
+    }
+  }
+  k_tv_out<<<g, 256, 0, s>>>(f, A[0], depth_out, n);
+  mh_count_launches(2 + iterations);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
