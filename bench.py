@@ -107,11 +107,13 @@ class ClockSampler:
                 "reasons": reasons, "gpu": gpu, "samples": len(rows)}
 
 
-def workload_params():
+def workload_params(capacity_log2=21):
     from meshhashing_gb300 import config, scene
     wl = scene.full_spline(8)
-    return config.params_for(wl, value_capacity=1 << 21, max_vertex_count=1 << 23, max_triangle_count=1 << 23,
-                             overflow_capacity=1 << 20)
+    pools = 1 << min(23, capacity_log2 + 2)
+    return config.params_for(wl, value_capacity=1 << capacity_log2, max_vertex_count=pools,
+                             max_triangle_count=pools, overflow_capacity=1 << 20,
+                             mesh_page_capacity=1 << (capacity_log2 - 3))
 
 
 def peaks():
@@ -123,16 +125,18 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def bytes_per_launch(stage, nb, px, rpx, vwork):
-    """Algorithmic bytes one launch of a stage must move."""
+def bytes_per_launch(stage, nb, px, rpx, vwork, cube_blocks=0, mesh_blocks=0, predict_blocks=0):
+    """Algorithmic bytes one launch of a stage must move (per-frame averages of
+    the blocks each kernel actually visits, counted on the device)."""
     if stage == "integrate":       # sdf, inv_sigma2, a, b read+write; depth + inlier images
         return nb * 512 * 32 + px * 8
-    if stage == "predict":         # three vertex slots per voxel, the inlier image
-        return nb * 512 * 12 + px * 4
+    if stage == "predict":         # vertex slots of blocks with vertices; the inlier image
+        return predict_blocks * 512 * 12 + px * 4
     if stage == "raycast":         # 2 KB sdf + 16 B entry per block in view; depth, vertex, normal out
         return nb * (512 * 4 + 16) + rpx * 36
-    if stage == "mesh":            # 9^3 corner tile (4 fields), cube index, claim, slots; vertices out
-        return nb * (729 * 16 + 512 * (1 + 4 + 12 + 20)) + vwork * 32
+    if stage == "mesh":            # 9^3 corner tile of 4 fields + cube bytes for tiled blocks;
+        # slots (12 + 20 B), cube and claim per voxel of paged blocks, twice; 32 B per vertex
+        return cube_blocks * (729 * 16 + 512) + mesh_blocks * 512 * (12 + 20 + 1 + 4) * 2 + vwork * 32
     if stage == "tv":
         return TV_ITERS * px * 36 + px * 24
     if stage == "alloc":
@@ -196,6 +200,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-frames", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--capacity-log2", type=int, default=21,
+                    help="block pool size (2^n blocks); smaller values for profiler captures")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -222,7 +228,7 @@ def main():
     from meshhashing_gb300 import Volume, launch_count
     from meshhashing_gb300 import build as B
     B.build()
-    params = workload_params()
+    params = workload_params(args.capacity_log2)
     vol = Volume(params)
     Hh, Ww = params.height, params.width
     dev_depth = torch.from_numpy(np.stack(frames[:P + W + K])).cuda()
@@ -290,18 +296,21 @@ def main():
     passes = max(s1["mesh_passes"] - s0["mesh_passes"], 1)
     nb = (s1["candidate_sum"] - s0["candidate_sum"]) / passes
     vwork = (s1["vertex_work_sum"] - s0["vertex_work_sum"]) / passes
+    counts = {"cube_blocks": (s1["cube_blocks_sum"] - s0["cube_blocks_sum"]) / passes,
+              "mesh_blocks": (s1["mesh_list_sum"] - s0["mesh_list_sum"]) / passes,
+              "predict_blocks": (s1["predict_blocks_sum"] - s0["predict_blocks_sum"]) / passes}
     px, rpx = Ww * Hh, params.rc_width * params.rc_height
     peak, peak_kind = peaks()
     stage_ms = {k: v[0] for k, v in prof.items()}
     dom = max(("integrate", "raycast", "predict", "alloc", "collect"), key=lambda k: stage_ms[k])
     calls = max(prof[dom][1], 1)
     per_launch_ms = stage_ms[dom] / calls
-    alg = bytes_per_launch(dom, nb, px, rpx, vwork)
+    alg = bytes_per_launch(dom, nb, px, rpx, vwork, **counts)
     achieved = alg / (per_launch_ms / 1000.0) / 1e9
     stages = {}
     for k, (t_ms, c) in prof.items():
         if c:
-            b = bytes_per_launch(k, nb, px, rpx, vwork)
+            b = bytes_per_launch(k, nb, px, rpx, vwork, **counts)
             gbs = b / ((t_ms / c) / 1000.0) / 1e9 if t_ms > 0 else None
             stages[k] = {"ms_per_frame": t_ms / K, "gbs": gbs, "frac": (gbs / peak) if gbs else None}
 
@@ -327,8 +336,9 @@ def main():
                             "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                             "bytes_per_launch": alg},
                "stages": stages,
-               "blocks": {"candidates_per_frame": nb, "vertices_per_frame": vwork,
-                          "allocated": s2["blocks_allocated"], "error": s2["error"]},
+               "blocks": {"candidates_per_frame": nb, "vertices_per_frame": vwork, **counts,
+                          "allocated": s2["blocks_allocated"], "mesh_pages": s2["mesh_pages_used"],
+                          "error": s2["error"]},
                "clocks": clocks,
                "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)

@@ -93,6 +93,10 @@ typedef struct mh_stats {
   uint32_t mesh_passes;           /* mh_mesh calls since reset */
   uint64_t candidate_sum;         /* candidate-list lengths summed over mesh passes */
   uint64_t vertex_work_sum;       /* vertices (re)computed, summed over mesh passes */
+  uint64_t cube_blocks_sum;       /* blocks whose corner tile the cube pass loaded */
+  uint64_t mesh_list_sum;         /* blocks walked by the triangle and recycle passes */
+  uint64_t predict_blocks_sum;    /* blocks the inlier prediction read */
+  uint32_t mesh_pages_used;       /* mesh pages held by blocks */
 } mh_stats;
 
 typedef struct mh_volume mh_volume;

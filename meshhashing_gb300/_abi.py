@@ -34,7 +34,9 @@ class MhStats(C.Structure):
     _fields_ = [(n, _u32) for n in (
         "error", "blocks_allocated", "block_high_water", "candidates", "vertices_allocated",
         "triangles_allocated", "overflow_used", "frames", "dropped_inserts", "gc_freed_blocks",
-        "mesh_passes")] + [("candidate_sum", C.c_uint64), ("vertex_work_sum", C.c_uint64)]
+        "mesh_passes")] + [(n, C.c_uint64) for n in (
+        "candidate_sum", "vertex_work_sum", "cube_blocks_sum", "mesh_list_sum", "predict_blocks_sum")] + [
+        ("mesh_pages_used", _u32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

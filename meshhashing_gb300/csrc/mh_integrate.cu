@@ -215,6 +215,7 @@ __global__ void __launch_bounds__(128) k_predict_inlier(Dev d) {
     const int4 *vs4 = reinterpret_cast<const int4 *>(d.vtx_slot + ((size_t)pg * MH_BLOCK_VOXELS + t * 4) * 3);
     int4 q0 = vs4[0], q1 = vs4[1], q2 = vs4[2];
     int slots[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+    if (t == 0) atomicAdd(&d.ctr->predict_blocks_sum, 1ull);
     bool has = false;
 #pragma unroll
     for (int k = 0; k < 12; ++k) has |= slots[k] > 0;

@@ -62,6 +62,9 @@ struct Counters {
   int mesh_list_count; // candidates holding a mesh page this pass
   unsigned long long cand_sum;   // sum of candidate counts over mesh calls
   unsigned long long vwork_sum;  // sum of computed vertices over mesh calls
+  unsigned long long cube_blocks_sum;     // blocks the cube pass loaded a tile for
+  unsigned long long mesh_list_sum;       // blocks the triangle/recycle passes walked
+  unsigned long long predict_blocks_sum;  // blocks the inlier prediction read
 };
 
 // Per-frame pose constants, kept in device memory so that captured graphs can

@@ -78,6 +78,7 @@ __global__ void k_mc_end(Dev d) {
   d.ctr->mesh_passes += 1;
   d.ctr->cand_sum += (unsigned long long)d.ctr->cand_count;
   d.ctr->vwork_sum += (unsigned long long)min(d.ctr->vwork_count, d.vwork_capacity);
+  d.ctr->mesh_list_sum += (unsigned long long)d.ctr->mesh_list_count;
 }
 
 // ------------------------------------------------------------------ pass 1
@@ -99,6 +100,7 @@ __global__ void __launch_bounds__(512) k_mc_cubes(Dev d) {
     if (tid < 8) {
       const int dx = tid & 1, dy = (tid >> 1) & 1, dz = tid >> 2;
       nb[tid] = tid == 0 ? cb.w : hash_find(d, cb.x + dx, cb.y + dy, cb.z + dz);
+      if (tid == 0) atomicAdd(&d.ctr->cube_blocks_sum, 1ull);
     }
     __syncthreads();
     for (int e = tid; e < 729; e += 512) {

@@ -563,6 +563,10 @@ int mh_stats_get(mh_volume *v, mh_stats *out, void *stream) {
   out->mesh_passes = (uint32_t)c.mesh_passes;
   out->candidate_sum = c.cand_sum;
   out->vertex_work_sum = c.vwork_sum;
+  out->cube_blocks_sum = c.cube_blocks_sum;
+  out->mesh_list_sum = c.mesh_list_sum;
+  out->predict_blocks_sum = c.predict_blocks_sum;
+  out->mesh_pages_used = (uint32_t)(v->d.page_capacity - c.page_top);
   return MH_OK;
 }
 
