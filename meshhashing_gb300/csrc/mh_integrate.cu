@@ -203,14 +203,12 @@ __global__ void __launch_bounds__(128) k_predict_inlier(Dev d) {
   if (threadIdx.x < 16) cTw[threadIdx.x] = d.fc->cTw[threadIdx.x];
   __syncthreads();
   const DevParams &p = d.p;
-  const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
+  const int n = *reinterpret_cast<volatile int *>(&d.ctr->vtx_list_count);
   const int t = threadIdx.x;
   const int lx = (t & 1) * 4, ly = (t >> 1) & 7, lz = t >> 4;
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
-    const int4 cb = d.cand[c];
-    if (cb.w < 0 || __ldg(d.nvtx + cb.w) <= 0) continue;
+    const int4 cb = d.cand[d.vtx_list[c]];
     const int pg = __ldg(d.page_of + cb.w);
-    if (pg < 0) continue;
     const size_t base = (size_t)cb.w * MH_BLOCK_VOXELS + t * 4;
     const int4 *vs4 = reinterpret_cast<const int4 *>(d.vtx_slot + ((size_t)pg * MH_BLOCK_VOXELS + t * 4) * 3);
     int4 q0 = vs4[0], q1 = vs4[1], q2 = vs4[2];
@@ -255,6 +253,26 @@ __global__ void __launch_bounds__(128) k_predict_inlier(Dev d) {
   }
 }
 
+// Candidates owning at least one vertex (and so a mesh page), for the
+// inlier prediction; one thread per candidate, warp-ballot compaction.
+__global__ void __launch_bounds__(256) k_vtx_select(Dev d) {
+  const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int i = base + threadIdx.x;
+    bool keep = false;
+    if (i < n) {
+      const int ptr = d.cand[i].w;
+      keep = ptr >= 0 && d.nvtx[ptr] > 0 && d.page_of[ptr] >= 0;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    int slot = 0;
+    if (lane_id() == 0 && m) slot = atomicAdd(&d.ctr->vtx_list_count, __popc(m));
+    slot = __shfl_sync(0xffffffffu, slot, 0);
+    if (keep) d.vtx_list[slot + __popc(m & lanemask_lt())] = i;
+  }
+}
+
 // Sensor::Process tail: depth validity (ConvertDepthFormatKernel,
 // sensor/preprocess.cu:25-42) and inlier-ratio reset to 0.1 (:10-23).
 __global__ void k_preprocess(Dev d, const float *src, const uint16_t *src16, float range_factor) {
@@ -280,8 +298,10 @@ int launch_integrate_psdf(const Dev &d, cudaStream_t s) {
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }
 int launch_predict_inlier(const Dev &d, cudaStream_t s) {
+  MH_CUDA_TRY(cudaMemsetAsync(&d.ctr->vtx_list_count, 0, sizeof(int), s));
+  k_vtx_select<<<grid_persistent(4), 256, 0, s>>>(d);
   k_predict_inlier<<<grid_persistent(12), 128, 0, s>>>(d);
-  mh_count_launches(1);
+  mh_count_launches(2);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }
 int launch_preprocess(const Dev &d, const float *src, const uint16_t *src16, float range_factor, cudaStream_t s) {

@@ -60,6 +60,9 @@ struct Counters {
   int mesh_passes;     // mesh calls since reset
   int page_top;        // free mesh pages
   int mesh_list_count; // candidates holding a mesh page this pass
+  int cube_list_count; // candidates the cube pass must tile this pass
+  int vtx_list_count;  // candidates owning vertices (inlier prediction)
+  int ray_next;        // next ray handed out by the raycast
   unsigned long long cand_sum;   // sum of candidate counts over mesh calls
   unsigned long long vwork_sum;  // sum of computed vertices over mesh calls
   unsigned long long cube_blocks_sum;     // blocks the cube pass loaded a tile for
@@ -112,6 +115,8 @@ struct Dev {
   int *page_heap;          // free pages
   int *page_owner;         // per page: block index or -1
   int *mesh_list;          // candidates holding a page (this mesh pass)
+  int4 *cube_list;         // candidates the cube pass tiles (x, y, z, block)
+  int *vtx_list;           // candidate indices owning vertices
   int page_capacity;
   Vertex *vtx;
   int *vtx_heap;
@@ -283,16 +288,22 @@ struct BlockCache {
 
 // GetSpatialValue (geometry/spatial_query.h:23-66): trilinear sdf (and the
 // interpolated sqrt(1/inv_sigma2) when want_radius); false if any corner
-// block is missing.
+// block is missing.  The block of corner 0 is looked up first, so a sample
+// inside a block already known to be missing costs three divisions and one
+// cache compare; corners in other blocks go through a second cache entry.
 template <bool want_radius>
-__device__ __forceinline__ bool spatial_sample(const Dev &d, BlockCache &bc, F3 pos, float &sdf, float &radius) {
+__device__ __forceinline__ bool spatial_sample(const Dev &d, BlockCache &bc, F3 pos, float &sdf, float &radius,
+                                               BlockCache *bc2 = nullptr) {
   const float off = d.p.voxel_size;
   const float vs = d.p.voxel_size;
-  F3 pc = f3(pos.x - 0.5f * off, pos.y - 0.5f * off, pos.z - 0.5f * off);
-  float qx = pos.x / vs, qy = pos.y / vs, qz = pos.z / vs;
-  float rx = qx - floorf(qx), ry = qy - floorf(qy), rz = qz - floorf(qz);
-  int v0x = w2vi(pc.x, vs), v0y = w2vi(pc.y, vs), v0z = w2vi(pc.z, vs);
-  int v1x = w2vi(pc.x + 1.0f * off, vs), v1y = w2vi(pc.y + 1.0f * off, vs), v1z = w2vi(pc.z + 1.0f * off, vs);
+  const F3 pc = f3(pos.x - 0.5f * off, pos.y - 0.5f * off, pos.z - 0.5f * off);
+  const int v0x = w2vi(pc.x, vs), v0y = w2vi(pc.y, vs), v0z = w2vi(pc.z, vs);
+  const int b0x = vox2blk(v0x), b0y = vox2blk(v0y), b0z = vox2blk(v0z);
+  const int p0 = bc.get(d, b0x, b0y, b0z);
+  if (p0 < 0) return false;
+  const int v1x = w2vi(pc.x + 1.0f * off, vs), v1y = w2vi(pc.y + 1.0f * off, vs), v1z = w2vi(pc.z + 1.0f * off, vs);
+  const float qx = pos.x / vs, qy = pos.y / vs, qz = pos.z / vs;
+  const float rx = qx - floorf(qx), ry = qy - floorf(qy), rz = qz - floorf(qz);
   float s = 0.0f, rad = 0.0f;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
@@ -300,8 +311,11 @@ __device__ __forceinline__ bool spatial_sample(const Dev &d, BlockCache &bc, F3 
     const int vx = mx ? v1x : v0x, vy = my ? v1y : v0y, vz = mz ? v1z : v0z;
     const float wx = mx ? rx : 1.0f - rx, wy = my ? ry : 1.0f - ry, wz = mz ? rz : 1.0f - rz;
     const int bx = vox2blk(vx), by = vox2blk(vy), bz = vox2blk(vz);
-    const int ptr = bc.get(d, bx, by, bz);
-    if (ptr < 0) return false;
+    int ptr = p0;
+    if (bx != b0x || by != b0y || bz != b0z) {
+      ptr = bc2 ? bc2->get(d, bx, by, bz) : hash_find(d, bx, by, bz);
+      if (ptr < 0) return false;
+    }
     const int li = (vx - bx * MH_BLOCK_SIDE) + (vy - by * MH_BLOCK_SIDE) * MH_BLOCK_SIDE +
                    (vz - bz * MH_BLOCK_SIDE) * MH_BLOCK_SIDE * MH_BLOCK_SIDE;
     const size_t gi = (size_t)ptr * MH_BLOCK_VOXELS + li;

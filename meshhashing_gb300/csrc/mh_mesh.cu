@@ -73,6 +73,31 @@ __global__ void k_mc_begin(Dev d) {
   d.ctr->epoch += 1;
   d.ctr->vwork_count = 0;
   d.ctr->mesh_list_count = 0;
+  d.ctr->cube_list_count = 0;
+}
+
+// Candidates the cube pass must tile: a block holding a mesh page, or one
+// whose weight bound reaches the MC gate (otherwise no cube in it is valid).
+// One thread per candidate, warp-ballot compaction.
+__global__ void __launch_bounds__(256) k_mc_select(Dev d) {
+  const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
+  const float lim = 1.0f / d.p.voxel_size;
+  const float lim2 = lim * lim;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int i = base + threadIdx.x;
+    int4 cb = make_int4(0, 0, 0, -1);
+    bool keep = false;
+    if (i < n) {
+      cb = d.cand[i];
+      keep = cb.w >= 0 && (d.page_of[cb.w] >= 0 || !(d.wmax[cb.w] < lim2));
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    int slot = 0;
+    if (lane_id() == 0 && m) slot = atomicAdd(&d.ctr->cube_list_count, __popc(m));
+    slot = __shfl_sync(0xffffffffu, slot, 0);
+    if (keep) d.cube_list[slot + __popc(m & lanemask_lt())] = cb;
+  }
 }
 __global__ void k_mc_end(Dev d) {
   d.ctr->mesh_passes += 1;
@@ -87,16 +112,13 @@ __global__ void __launch_bounds__(512) k_mc_cubes(Dev d) {
   __shared__ int nb[8];
   __shared__ int own_page;
   const int tid = threadIdx.x;
-  const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
+  const int n = *reinterpret_cast<volatile int *>(&d.ctr->cube_list_count);
   const unsigned epoch = *reinterpret_cast<volatile unsigned *>(&d.ctr->epoch);
   const float lim = 1.0f / d.p.voxel_size;
   const float lim2 = lim * lim;
   const int x = tid & 7, y = (tid >> 3) & 7, z = tid >> 6;
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
-    const int4 cb = d.cand[c];
-    if (cb.w < 0) continue;
-    // no page and no voxel that can pass the weight gate: no valid cube
-    if (d.page_of[cb.w] < 0 && d.wmax[cb.w] < lim2) continue;
+    const int4 cb = d.cube_list[c];
     if (tid < 8) {
       const int dx = tid & 1, dy = (tid >> 1) & 1, dz = tid >> 2;
       nb[tid] = tid == 0 ? cb.w : hash_find(d, cb.x + dx, cb.y + dy, cb.z + dz);
@@ -397,6 +419,7 @@ __global__ void __launch_bounds__(128) k_mc_recycle_vtx(Dev d) {
 int launch_mesh(const Dev &d, cudaStream_t s) {
   const int sms = mh_sm_count();
   k_mc_begin<<<1, 1, 0, s>>>(d);
+  k_mc_select<<<sms * 4, 256, 0, s>>>(d);
   k_mc_cubes<<<sms * 2, 512, 0, s>>>(d);
   k_mc_list<<<sms * 4, 256, 0, s>>>(d);
   k_mc_vertices<<<sms * 8, 128, 0, s>>>(d);
@@ -404,6 +427,6 @@ int launch_mesh(const Dev &d, cudaStream_t s) {
   k_mc_recycle_tri<<<sms * 8, 128, 0, s>>>(d);
   k_mc_recycle_vtx<<<sms * 8, 128, 0, s>>>(d);
   k_mc_end<<<1, 1, 0, s>>>(d);
-  mh_count_launches(8);
+  mh_count_launches(9);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }

@@ -322,6 +322,8 @@ int mh_volume_create(const mh_params *p, mh_volume **out) {
   A(dalloc(v, &d.page_of, cap));
   A(dalloc(v, &d.wmax, cap));
   A(dalloc(v, &d.mesh_list, cap));
+  A(dalloc(v, &d.cube_list, cap));
+  A(dalloc(v, &d.vtx_list, cap));
   A(dalloc(v, &d.page_heap, (size_t)d.page_capacity));
   A(dalloc(v, &d.page_owner, (size_t)d.page_capacity));
   A(dalloc(v, &d.vtx_slot, pv * 3));

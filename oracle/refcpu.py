@@ -1,0 +1,171 @@
+"""TEST INFRASTRUCTURE: the reference's own device code built for the CPU.
+
+``build(ref_root)`` extracts the reference's kernels (refcpu/extract.py) and
+compiles them with refcpu/refcpu.cpp into oracle/_ref/librefcpu.so; it needs
+the reference tree, so it runs only where that tree is present (this is how
+tests/golden/ fixtures are produced; see tests/golden/make_golden.py).
+``RefCPU`` drives the reference's stages (AllocBlockArray,
+CollectBlocksInFrustum, UpdateBlocksSimple / Bayesian, MarchingCubes, GC,
+RayCaster::Cast) with the reference's launch shapes, one emulated CUDA
+thread at a time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT_DIR = os.path.join(HERE, "_ref")
+LIB = os.path.join(OUT_DIR, "librefcpu.so")
+
+
+def build(ref_root: str = "/root/reference", force: bool = False) -> str:
+    src = os.path.join(HERE, "refcpu", "refcpu.cpp")
+    deps = [src, os.path.join(HERE, "refcpu", "cuda_host.h"), os.path.join(HERE, "refcpu", "extract.py")]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
+        return LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    gen = os.path.join(OUT_DIR, "ref_kernels.inc")
+    subprocess.check_call([sys.executable, os.path.join(HERE, "refcpu", "extract.py"), ref_root, gen],
+                          stdout=subprocess.DEVNULL)
+    cuda_inc = "/usr/local/cuda/include"
+    cmd = ["g++", "-O2", "-std=c++14", "-ffp-contract=off", "-fPIC", "-shared", "-w",
+           "-I", os.path.join(HERE, "refcpu", "stubs"), "-I", os.path.join(ref_root, "src"),
+           "-I", os.path.join(ref_root, "src", "extern", "cuda"), "-I", cuda_inc,
+           "-I", OUT_DIR, "-I", os.path.join(HERE, "refcpu"), "-o", LIB + ".tmp", src]
+    subprocess.check_call(cmd)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(LIB)
+        vp, i32p, f32p = C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_float)
+        L.ref_create.restype = vp
+        L.ref_create.argtypes = [vp]
+        L.ref_destroy.argtypes = [vp]
+        L.ref_frame_set.argtypes = [vp, f32p, f32p]
+        L.ref_alloc.restype = C.c_int
+        L.ref_alloc.argtypes = [vp, C.c_int]
+        for n in ("ref_collect", "ref_allocated"):
+            getattr(L, n).restype = C.c_int
+            getattr(L, n).argtypes = [vp]
+        for n in ("ref_integrate_simple", "ref_predict", "ref_integrate_psdf", "ref_mesh", "ref_gc_low_surfel",
+                  "ref_gc_recycle"):
+            getattr(L, n).argtypes = [vp]
+        L.ref_raycast.argtypes = [vp, f32p, f32p, f32p]
+        L.ref_get_blocks.restype = C.c_int
+        L.ref_get_blocks.argtypes = [vp, C.c_int, i32p, f32p, f32p, f32p, f32p]
+        L.ref_get_candidates.restype = C.c_int
+        L.ref_get_candidates.argtypes = [vp, C.c_int, i32p]
+        L.ref_get_inlier.argtypes = [vp, f32p]
+        L.ref_dump_mesh.argtypes = [vp, C.c_int, i32p, f32p, C.c_int, i32p, i32p, i32p]
+        L.ref_inverse.argtypes = [f32p, f32p]
+        L.ref_cube_indices.argtypes = [vp, C.c_int, i32p, C.POINTER(C.c_uint8)]
+        _lib = L
+    return _lib
+
+
+def _p(a, ct):
+    return None if a is None else a.ctypes.data_as(C.POINTER(ct))
+
+
+def inverse(m):
+    a = np.ascontiguousarray(m, np.float32).reshape(16)
+    out = np.zeros(16, np.float32)
+    lib().ref_inverse(_p(a, C.c_float), _p(out, C.c_float))
+    return out.reshape(4, 4)
+
+
+class RefCPU:
+    def __init__(self, params):
+        self.p = params
+        self.L = lib()
+        self.h = self.L.ref_create(C.byref(params))
+
+    def __del__(self):
+        try:
+            self.L.ref_destroy(self.h)
+        except Exception:
+            pass
+
+    def frame_set(self, depth, wTc):
+        d = np.ascontiguousarray(depth, np.float32).reshape(-1)
+        m = np.ascontiguousarray(wTc, np.float32).reshape(16)
+        self.L.ref_frame_set(self.h, _p(d, C.c_float), _p(m, C.c_float))
+
+    def alloc(self, until_stable=True):
+        return self.L.ref_alloc(self.h, 1 if until_stable else 0)
+
+    def collect(self):
+        return self.L.ref_collect(self.h)
+
+    def integrate_simple(self):
+        self.L.ref_integrate_simple(self.h)
+
+    def predict(self):
+        self.L.ref_predict(self.h)
+
+    def integrate_psdf(self):
+        self.L.ref_integrate_psdf(self.h)
+
+    def mesh(self):
+        self.L.ref_mesh(self.h)
+
+    def gc_low_surfel(self):
+        self.L.ref_gc_low_surfel(self.h)
+
+    def gc_recycle(self):
+        self.L.ref_gc_recycle(self.h)
+
+    def raycast(self, cTw):
+        W, H = self.p.rc_width, self.p.rc_height
+        d = np.zeros(W * H, np.float32)
+        n = np.zeros(W * H * 4, np.float32)
+        m = np.ascontiguousarray(cTw, np.float32).reshape(16)
+        self.L.ref_raycast(self.h, _p(m, C.c_float), _p(d, C.c_float), _p(n, C.c_float))
+        return d.reshape(H, W), n.reshape(H, W, 4)
+
+    def blocks(self):
+        n = self.L.ref_get_blocks(self.h, 0, None, None, None, None, None)
+        pos = np.zeros((max(n, 1), 3), np.int32)
+        arrs = [np.zeros((max(n, 1), 512), np.float32) for _ in range(4)]
+        self.L.ref_get_blocks(self.h, n, _p(pos, C.c_int32), *[_p(a, C.c_float) for a in arrs])
+        return (pos[:n],) + tuple(a[:n] for a in arrs)
+
+    def candidates(self):
+        n = self.L.ref_get_candidates(self.h, 0, None)
+        out = np.zeros((max(n, 1), 3), np.int32)
+        self.L.ref_get_candidates(self.h, n, _p(out, C.c_int32))
+        return out[:n]
+
+    def inlier(self):
+        out = np.zeros(self.p.width * self.p.height, np.float32)
+        self.L.ref_get_inlier(self.h, _p(out, C.c_float))
+        return out.reshape(self.p.height, self.p.width)
+
+    def dump_mesh(self):
+        nv, nt = C.c_int32(0), C.c_int32(0)
+        self.L.ref_dump_mesh(self.h, 0, None, None, 0, None, C.byref(nv), C.byref(nt))
+        vk = np.zeros((max(nv.value, 1), 4), np.int32)
+        vd = np.zeros((max(nv.value, 1), 8), np.float32)
+        tr = np.zeros((max(nt.value, 1), 7), np.int32)
+        a, b = nv.value, nt.value
+        self.L.ref_dump_mesh(self.h, a, _p(vk, C.c_int32), _p(vd, C.c_float), b, _p(tr, C.c_int32),
+                             C.byref(nv), C.byref(nt))
+        return vk[:a], vd[:a], tr[:b]
+
+    def cubes(self, pos):
+        pos = np.ascontiguousarray(pos, np.int32).reshape(-1, 3)
+        out = np.zeros((len(pos), 512), np.uint8)
+        self.L.ref_cube_indices(self.h, len(pos), _p(pos, C.c_int32), out.ctypes.data_as(C.POINTER(C.c_uint8)))
+        return out
