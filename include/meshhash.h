@@ -77,6 +77,11 @@ typedef struct mh_params {
   uint32_t mesh_page_capacity;    /* mesh pages (per-voxel mesh units of one
                                      block, 18.5 KB); only blocks with surface
                                      cubes or owned vertices take one */
+  int32_t  compat_arithmetic;     /* 1: evaluate the reference's single-precision
+                                     formulas as written (results bit-compatible
+                                     with the reference's own kernels);
+                                     0: well-conditioned equivalent forms of the
+                                     two that cancel (default) */
 } mh_params;
 
 typedef struct mh_stats {

@@ -23,7 +23,7 @@ class MhParams(C.Structure):
         ("min_raycast_depth", _f32), ("max_raycast_depth", _f32), ("raycast_step", _f32),
         ("sample_sdf_threshold", _f32), ("sdf_threshold", _f32), ("enable_gradients", _i32),
         ("enable_bayesian_update", _i32), ("enable_sdf_gradient", _i32),
-        ("overflow_capacity", _u32), ("mesh_page_capacity", _u32),
+        ("overflow_capacity", _u32), ("mesh_page_capacity", _u32), ("compat_arithmetic", _i32),
     ]
 
     def as_dict(self):

@@ -11,7 +11,7 @@ from ._abi import MhParams
 def make_params(width, height, fx, fy, cx, cy, voxel_size, truncation, bayesian,
                 bucket_count, value_capacity, weight_sample=10, max_vertex_count=1 << 22,
                 max_triangle_count=1 << 22, overflow_capacity=None, raycast_step=None,
-                linked_list_size=7, mesh_page_capacity=None) -> MhParams:
+                linked_list_size=7, mesh_page_capacity=None, compat_arithmetic=0) -> MhParams:
     p = MhParams()
     p.bucket_count = bucket_count
     p.bucket_size = 4
@@ -39,6 +39,7 @@ def make_params(width, height, fx, fy, cx, cy, voxel_size, truncation, bayesian,
     p.enable_bayesian_update = 1 if bayesian else 0
     p.enable_sdf_gradient = 1
     p.overflow_capacity = overflow_capacity if overflow_capacity is not None else max(bucket_count // 4, 1024)
+    p.compat_arithmetic = compat_arithmetic
     p.mesh_page_capacity = (mesh_page_capacity if mesh_page_capacity is not None
                             else max(min(value_capacity, 1 << 20) // 2, min(value_capacity, 1024)))
     return p

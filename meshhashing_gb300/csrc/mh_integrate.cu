@@ -77,8 +77,10 @@ __global__ void __launch_bounds__(128) k_integrate_simple(Dev d) {
       if (!project_voxel(p, cTw, d.depth, vx0 + k, vy, vz, o)) continue;
       float sdf = o.depth - o.cam_z;
       // 1 - normalized depth as (dmax - d) / (dmax - dmin): same value, no
-      // cancellation near the far limit (update_simple.cu:49-55)
-      const float far = (p.max_depth_range - o.depth) / (p.max_depth_range - p.min_depth_range);
+      // cancellation near the far limit (update_simple.cu:49-55); the
+      // compatibility mode keeps the reference's 1 - (d - dmin) / (dmax - dmin)
+      const float far = p.compat ? 1.0f - normalize_depth(p, o.depth)
+                                 : (p.max_depth_range - o.depth) / (p.max_depth_range - p.min_depth_range);
       const float w = fmaxf(10.0f * p.weight_sample * far, 1.0f);
       const float tr = truncate_dist(p, o.depth);
       if (sdf <= -tr) continue;
@@ -168,7 +170,16 @@ __global__ void __launch_bounds__(128) k_integrate_psdf(Dev d) {
       const float t2 = tau * tau;
       const float ss2 = 1.0f / (1.0f / s2 + 1.0f / t2);
       const float m = ss2 * (mu / s2 + x / t2);
-      float C1 = r * gaussianf(x, mu, s2 + t2);
+      float C1;
+      if (p.compat) {
+        // as the reference evaluates it: sqrt(2 pi) in double, so the product
+        // and the reciprocal are double (geometry_helper.h:30-34)
+        const float sv = s2 + t2;
+        const double g = 1.0 / (2.5066282746310002 * (double)sqrtf(sv)) * (double)expf(-((x - mu) * (x - mu)) / sv);
+        C1 = (float)((double)r * g);
+      } else {
+        C1 = r * gaussianf(x, mu, s2 + t2);
+      }
       float C2 = (dd < p.max_depth_range && dd >= p.min_depth_range) ? (1.0f - r) * 1.0f / (5.0f - 0.1f) : 1.0f;
       const float sum = C1 + C2;
       C1 /= sum;
@@ -178,7 +189,8 @@ __global__ void __launch_bounds__(128) k_integrate_psdf(Dev d) {
       const float e = C1 * (a + 1) * (a + 2) / ((a + b + 1) * (a + b + 2)) + C2 * a * (a + 1) / ((a + b + 1) * (a + b + 2));
       const float nsdf = C1 * m + C2 * mu;
       const float dm = m - mu;
-      const float var = C1 * ss2 + C2 * s2 + C1 * C2 * (dm * dm);
+      const float var = p.compat ? C1 * (ss2 + m * m) + C2 * (s2 + mu * mu) - nsdf * nsdf
+                                 : C1 * ss2 + C2 * s2 + C1 * C2 * (dm * dm);
       put(S, k, nsdf);
       put(W, k, 1.0f / var);
       const float na = (e - f) / (f - e / f);

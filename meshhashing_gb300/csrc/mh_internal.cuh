@@ -93,6 +93,7 @@ struct DevParams {
   uint32_t rc_width, rc_height;
   float min_raycast_depth, max_raycast_depth, raycast_step, sample_sdf_threshold, sdf_threshold;
   int enable_gradients, enable_bayesian;
+  int compat;  // evaluate the reference's formulas as written
 };
 
 // Everything a kernel needs, passed by value (pointers + params).
@@ -286,6 +287,19 @@ struct BlockCache {
   }
 };
 
+// Corner voxel indices of one axis for GetSpatialValue: exactly
+// WorldToVoxeli(p - v/2) and WorldToVoxeli(p - v/2 + v).
+__device__ __forceinline__ void corner_pair(float p, float off, float vs, float fl, float fr, int &c0, int &c1) {
+  if (fr > 0.01f && fr < 0.99f) {
+    c0 = (int)fl;
+    c1 = c0 + 1;
+  } else {
+    const float pc = p - 0.5f * off;
+    c0 = w2vi(pc, vs);
+    c1 = w2vi(pc + 1.0f * off, vs);
+  }
+}
+
 // GetSpatialValue (geometry/spatial_query.h:23-66): trilinear sdf (and the
 // interpolated sqrt(1/inv_sigma2) when want_radius); false if any corner
 // block is missing.  The block of corner 0 is looked up first, so a sample
@@ -296,14 +310,19 @@ __device__ __forceinline__ bool spatial_sample(const Dev &d, BlockCache &bc, F3 
                                                BlockCache *bc2 = nullptr) {
   const float off = d.p.voxel_size;
   const float vs = d.p.voxel_size;
-  const F3 pc = f3(pos.x - 0.5f * off, pos.y - 0.5f * off, pos.z - 0.5f * off);
-  const int v0x = w2vi(pc.x, vs), v0y = w2vi(pc.y, vs), v0z = w2vi(pc.z, vs);
+  const float qx = pos.x / vs, qy = pos.y / vs, qz = pos.z / vs;
+  const float fx = floorf(qx), fy = floorf(qy), fz = floorf(qz);
+  const float rx = qx - fx, ry = qy - fy, rz = qz - fz;
+  // The corner voxels are round-half-away((p - v/2)/v) and ((p + v/2)/v), which
+  // equal floor(p/v) and floor(p/v) + 1 unless p/v lies within rounding error
+  // of an integer; only there are the two extra divisions evaluated.
+  int v0x, v0y, v0z, v1x, v1y, v1z;
+  corner_pair(pos.x, off, vs, fx, rx, v0x, v1x);
+  corner_pair(pos.y, off, vs, fy, ry, v0y, v1y);
+  corner_pair(pos.z, off, vs, fz, rz, v0z, v1z);
   const int b0x = vox2blk(v0x), b0y = vox2blk(v0y), b0z = vox2blk(v0z);
   const int p0 = bc.get(d, b0x, b0y, b0z);
   if (p0 < 0) return false;
-  const int v1x = w2vi(pc.x + 1.0f * off, vs), v1y = w2vi(pc.y + 1.0f * off, vs), v1z = w2vi(pc.z + 1.0f * off, vs);
-  const float qx = pos.x / vs, qy = pos.y / vs, qz = pos.z / vs;
-  const float rx = qx - floorf(qx), ry = qy - floorf(qy), rz = qz - floorf(qz);
   float s = 0.0f, rad = 0.0f;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {

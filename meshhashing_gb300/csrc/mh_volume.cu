@@ -28,9 +28,20 @@ struct mh_volume {
   bool has_frame = false;
   int frames = 0;
   std::vector<void *> allocs;
-  // per-stage CUDA-event timing
+  // per-stage CUDA-event timing (events are pooled and reused)
   bool prof = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pend[MH_STAGE_COUNT];
+  std::vector<cudaEvent_t> ev_pool;
+  cudaEvent_t event() {
+    cudaEvent_t e = nullptr;
+    if (!ev_pool.empty()) {
+      e = ev_pool.back();
+      ev_pool.pop_back();
+    } else {
+      cudaEventCreate(&e);
+    }
+    return e;
+  }
 };
 
 static std::atomic<unsigned long long> g_launches{0};
@@ -44,8 +55,8 @@ struct StageScope {
   cudaEvent_t a = nullptr, b = nullptr;
   StageScope(mh_volume *v_, int st, cudaStream_t s_) : v(v_), stage(st), s(s_) {
     if (!v->prof) return;
-    cudaEventCreate(&a);
-    cudaEventCreate(&b);
+    a = v->event();
+    b = v->event();
     cudaEventRecord(a, s);
   }
   ~StageScope() {
@@ -296,6 +307,7 @@ int mh_volume_create(const mh_params *p, mh_volume **out) {
   q.raycast_step = P.raycast_step;
   q.sample_sdf_threshold = P.sample_sdf_threshold, q.sdf_threshold = P.sdf_threshold;
   q.enable_gradients = P.enable_gradients, q.enable_bayesian = P.enable_bayesian_update;
+  q.compat = P.compat_arithmetic != 0;
 
   const size_t cap = P.value_capacity, nv = cap * MH_BLOCK_VOXELS, npix = (size_t)P.width * P.height;
   const size_t rpix = (size_t)P.rc_width * P.rc_height;
@@ -356,6 +368,9 @@ int mh_volume_create(const mh_params *p, mh_volume **out) {
 int mh_volume_destroy(mh_volume *v) {
   CHECK_VOL(v);
   cudaDeviceSynchronize();
+  for (auto &pv : v->pend)
+    for (auto &pr : pv) v->ev_pool.push_back(pr.first), v->ev_pool.push_back(pr.second);
+  for (cudaEvent_t e : v->ev_pool) cudaEventDestroy(e);
   for (void *p : v->allocs) cudaFree(p);
   if (v->scratch) cudaFree(v->scratch);
   delete v;
@@ -831,8 +846,8 @@ int mh_profile_read(mh_volume *v, double ms[MH_STAGE_COUNT], int calls[MH_STAGE_
       float t = 0.0f;
       cudaEventElapsedTime(&t, pr.first, pr.second);
       acc += t;
-      cudaEventDestroy(pr.first);
-      cudaEventDestroy(pr.second);
+      v->ev_pool.push_back(pr.first);
+      v->ev_pool.push_back(pr.second);
     }
     if (ms) ms[st] = acc;
     if (calls) calls[st] = (int)v->pend[st].size();

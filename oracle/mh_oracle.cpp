@@ -532,7 +532,7 @@ template <class R> struct Vol {
         // mode evaluates 1 - nd as (dmax - d) / (dmax - dmin), which is exact in
         // the subtraction near the far limit where 1 - nd cancels.
         R w;
-        if (sizeof(R) == 8) {
+        if (sizeof(R) == 8 || p.compat_arithmetic) {
           R nd = normalize_depth(d);
           w = std::max((R)10 * (R)p.weight_sample * ((R)1 - nd), (R)1);
         } else {
@@ -640,7 +640,16 @@ template <class R> struct Vol {
         R t2 = tau * tau;
         R ss2 = (R)1 / ((R)1 / s2 + (R)1 / t2);
         R m = ss2 * (mu / s2 + x / t2);
-        R C1 = rho * gaussian(x, mu, s2 + t2);
+        R C1;
+        if (sizeof(R) == 4 && p.compat_arithmetic) {
+          // the reference's promotion: sqrt(2 pi) is a double (geometry_helper.h:30-34)
+          const float sv = (float)(s2 + t2);
+          const double g = 1.0 / (2.5066282746310002 * (double)std::sqrt(sv)) *
+                           (double)std::exp(-(((float)x - (float)mu) * ((float)x - (float)mu)) / sv);
+          C1 = (R)((double)rho * g);
+        } else {
+          C1 = rho * gaussian(x, mu, s2 + t2);
+        }
         R C2 = (d < (R)p.max_depth_range && d >= (R)p.min_depth_range) ? ((R)1 - rho) * (R)1 / ((R)5 - (R)0.1f)
                                                                          : (R)1;
         R sum = C1 + C2;
@@ -651,7 +660,7 @@ template <class R> struct Vol {
         R e = C1 * (a + 1) * (a + 2) / ((a + bb + 1) * (a + bb + 2)) + C2 * a * (a + 1) / ((a + bb + 1) * (a + bb + 2));
         R nsdf = C1 * m + C2 * mu;
         R var;
-        if (sizeof(R) == 8) {
+        if (sizeof(R) == 8 || p.compat_arithmetic) {
           var = C1 * (ss2 + m * m) + C2 * (s2 + mu * mu) - nsdf * nsdf;
         } else {
           R dm = m - mu;

@@ -1,0 +1,121 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+The reference has no tests or golden vectors, so its own device code, built
+for the CPU (oracle/refcpu: the reference's kernels and headers compiled with
+g++ against a CUDA-emulation shim), is run on small seeded inputs through
+the MainEngine stage order, and its outputs are stored together with the
+inputs.  Needs the reference tree (default /root/reference); the fixtures are
+committed, so tests never need the tree.
+
+  simple_room96.npz  plain TSDF chain, 96x72, 8 mm voxels, 6 frames of the
+                     circle trajectory: block sets, candidates, voxel values
+                     of sampled blocks, marching-cubes mesh, cube indices,
+                     raycast depth and normals
+  psdf_room96.npz    PSDF chain, 96x72, 4 mm voxels, 6 frames of the spline
+                     trajectory (with outliers and missing pixels): block
+                     set, voxel values of sampled blocks, inlier ratios
+
+Both use params.compat_arithmetic = 1 (the reference's single-precision
+formulas as written).  Allocation is repeated until no block is added, which
+removes the reference's per-bucket insert drops (the comparison target is the
+full touched set).
+
+Usage: python tests/golden/make_golden.py [reference root]
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from meshhashing_gb300 import config, scene  # noqa: E402
+
+N_SAMPLE = 32
+
+
+def simple_case():
+    wl = scene.small_circle(60)
+    f = 262.5 * 96 / 320
+    wl.camera = scene.Camera(96, 72, f, f, 47.5, 35.5)
+    frames = [0, 3, 6, 9, 12, 15]
+    p = config.params_for(wl, value_capacity=1 << 14, bucket_count=1 << 14, max_vertex_count=1 << 16,
+                          max_triangle_count=1 << 16, weight_sample=1000, compat_arithmetic=1)
+    depth = np.stack([wl.frame(i) for i in frames])
+    poses = np.stack([wl.pose(i) for i in frames])
+    return p, depth, poses
+
+
+def psdf_case():
+    wl = scene.full_spline(40, width=96, height=72)
+    frames = [0, 1, 2, 3, 4, 5]
+    p = config.params_for(wl, value_capacity=1 << 15, bucket_count=1 << 17, max_vertex_count=1 << 16,
+                          max_triangle_count=1 << 16, compat_arithmetic=1)
+    depth = np.stack([wl.frame(i) for i in frames])
+    poses = np.stack([wl.pose(i) for i in frames])
+    return p, depth, poses
+
+
+def sample_blocks(pos, w):
+    """Deterministic sample: the blocks with the most observed voxels."""
+    key = np.lexsort((pos[:, 2], pos[:, 1], pos[:, 0]))
+    obs = (w[key] > 0).sum(axis=1)
+    order = key[np.argsort(-obs, kind="stable")]
+    return order[:N_SAMPLE]
+
+
+def run_simple(ref_mod, p, depth, poses):
+    r = ref_mod.RefCPU(p)
+    counts = []
+    for d, T in zip(depth, poses):
+        r.frame_set(d, T)
+        counts.append(r.alloc(True))
+        r.collect()
+        r.integrate_simple()
+        r.mesh()
+        r.gc_low_surfel()
+    cand = r.candidates()
+    pos, s, w, _, _ = r.blocks()
+    idx = sample_blocks(pos, w)
+    vk, vd, tr = r.dump_mesh()
+    cTw = np.linalg.inv(poses[-1].astype(np.float64)).astype(np.float32)
+    rd, rn = r.raycast(cTw)
+    return dict(depth=depth, poses=poses, counts=np.array(counts, np.int32), blocks=pos, candidates=cand,
+                sample_pos=pos[idx], sample_sdf=s[idx], sample_w=w[idx], cubes=r.cubes(pos[idx]),
+                vkeys=vk, vpos=vd[:, :3], vref=vd[:, 7].astype(np.int32), tris=tr, ray_cTw=cTw, ray_depth=rd,
+                ray_normal=rn[..., :3])
+
+
+def run_psdf(ref_mod, p, depth, poses):
+    r = ref_mod.RefCPU(p)
+    counts = []
+    for d, T in zip(depth, poses):
+        r.frame_set(d, T)
+        counts.append(r.alloc(True))
+        r.collect()
+        r.predict()
+        r.integrate_psdf()
+        r.mesh()
+        r.gc_low_surfel()
+    pos, s, w, a, b = r.blocks()
+    idx = sample_blocks(pos, w)
+    return dict(depth=depth, poses=poses, counts=np.array(counts, np.int32), blocks=pos, sample_pos=pos[idx],
+                sample_sdf=s[idx], sample_w=w[idx], sample_a=a[idx], sample_b=b[idx], inlier=r.inlier())
+
+
+def main():
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    from oracle import refcpu
+    refcpu.build(ref_root)
+    p, depth, poses = simple_case()
+    np.savez_compressed(os.path.join(HERE, "simple_room96.npz"), **run_simple(refcpu, p, depth, poses))
+    p, depth, poses = psdf_case()
+    np.savez_compressed(os.path.join(HERE, "psdf_room96.npz"), **run_psdf(refcpu, p, depth, poses))
+    for f in ("simple_room96.npz", "psdf_room96.npz"):
+        print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
+
+
+if __name__ == "__main__":
+    main()
