@@ -11,20 +11,21 @@
 // GB300 structure.  The march is bound by instruction issue and by the
 // latency of its dependent loads, not by HBM bandwidth, so the work per
 // sample is what is cut, never the sample sequence itself:
+//  * one gather for every sample: the eight corners' blocks come from a
+//    per-ray table of the first corner block's 2x2x2 neighbourhood, filled by
+//    hash lookups only when a sample first needs an entry.  Samples whose
+//    corners straddle a block face take the same instructions as the others,
+//    so the lanes of a warp stay together (a separate slow path for the third
+//    of samples that straddle a face cost 1.45x in time).
 //  * one out-of-line sampler serves the march, the refinement and the
 //    gradient.  Inlined three times the kernel outgrew the instruction cache
-//    and needed 78 registers; out of line it runs in 64 (measured 4.9 ms ->
-//    3.2 ms per 640x480 frame on the 4 mm PSDF room).
+//    and its register budget (measured 1.5x slower).
 //  * empty-space skip: when the block holding a sample's first corner is
 //    missing, every later sample of the ray whose first corner falls in that
 //    block fails the same way.  The t interval in which the ray stays inside
 //    the block shrunk by a margin (0.1 voxel plus the float error of the
 //    position) is computed once, and samples inside it only advance t
 //    (t += step, the same accumulation as the full loop).
-//  * single-block fast path: when all eight corners lie in the first
-//    corner's block (7 of 8 voxel positions per axis) the eight values are
-//    read at fixed offsets from one base; otherwise a second cached lookup
-//    serves the neighbouring blocks.
 //  * 16x8-pixel CTAs keep neighbouring rays in one warp; they walk the same
 //    blocks at about the same t.
 #include "mh_internal.cuh"
@@ -36,20 +37,25 @@
 namespace {
 
 struct RayCache {
-  int bx, by, bz, ptr;  // block of the first corner of the last sample
-  int ox, oy, oz, optr; // last neighbouring block
+  int bx, by, bz;  // block of the first corner of the last sample
+  int valid;       // bit n: p[n] holds the lookup of block (bx, by, bz) + (n & 1, n >> 1 & 1, n >> 2 & 1)
+  int p[8];
   __device__ __forceinline__ void init() {
-    bx = by = bz = ox = oy = oz = 0x7fffffff;
-    ptr = optr = -1;
+    bx = by = bz = 0x7fffffff;
+    valid = 0;
   }
 };
 
 enum { RS_OK = 0, RS_MISS0 = 1, RS_MISS0_NEW = 2, RS_MISS = 3 };
 
 // GetSpatialValue (geometry/spatial_query.h:23-66) for the raycast: the same
-// corners, weights and summation order as spatial_sample.  Returns RS_OK, or
-// why the sample failed: its first corner's block is missing (RS_MISS0_NEW
-// when that block was just looked up) or another corner's block is missing.
+// corners, weights and summation order as spatial_sample.  Every sample runs
+// the same gather: corner i lies in block b0 + (mx & ex, my & ey, mz & ez),
+// where e is the block step between the two corner voxels of each axis, and
+// the up to eight blocks of b0's 2x2x2 neighbourhood are looked up once per
+// b0 and only when a sample needs them.  Returns RS_OK, or why the sample
+// failed: its first corner's block is missing (RS_MISS0_NEW when that block
+// was just looked up) or another corner's block is missing.
 __device__ __noinline__ int ray_sample(const Dev &d, RayCache &c, F3 pos, float &sdf) {
   const float off = d.p.voxel_size;
   const float vs = d.p.voxel_size;
@@ -61,45 +67,41 @@ __device__ __noinline__ int ray_sample(const Dev &d, RayCache &c, F3 pos, float 
   corner_pair(pos.y, off, vs, fy, ry, v0y, v1y);
   corner_pair(pos.z, off, vs, fz, rz, v0z, v1z);
   const int b0x = vox2blk(v0x), b0y = vox2blk(v0y), b0z = vox2blk(v0z);
-  int fresh = 0;
   if (b0x != c.bx || b0y != c.by || b0z != c.bz) {
     c.bx = b0x, c.by = b0y, c.bz = b0z;
-    c.ptr = hash_find(d, b0x, b0y, b0z);
-    fresh = 1;
+    c.valid = 0;
   }
-  if (c.ptr < 0) return fresh ? RS_MISS0_NEW : RS_MISS0;
+  const int ex = vox2blk(v1x) - b0x, ey = vox2blk(v1y) - b0y, ez = vox2blk(v1z) - b0z;
+  // blocks the eight corners use: every subset of the axes that step
+  int need = 1;
+  if (ex) need |= need << 1;
+  if (ey) need |= need << 2;
+  if (ez) need |= need << 4;
+  const int fresh = need & ~c.valid;
+  if (fresh & 1) c.p[0] = hash_find(d, b0x, b0y, b0z);
+  c.valid |= fresh & 1;
+  if (c.p[0] < 0) return (fresh & 1) ? RS_MISS0_NEW : RS_MISS0;
+  for (int todo = fresh & ~1; todo; todo &= todo - 1) {
+    const int n = __ffs(todo) - 1;
+    c.p[n] = hash_find(d, b0x + (n & 1), b0y + ((n >> 1) & 1), b0z + ((n >> 2) & 1));
+  }
+  c.valid |= fresh;
+  for (int m = need & ~1; m; m &= m - 1)
+    if (c.p[__ffs(m) - 1] < 0) return RS_MISS;
   const float w0x = 1.0f - rx, w0y = 1.0f - ry, w0z = 1.0f - rz;
-  const int lx = v0x - b0x * MH_BLOCK_SIDE, ly = v0y - b0y * MH_BLOCK_SIDE, lz = v0z - b0z * MH_BLOCK_SIDE;
+  // local voxel coordinates of the two corners of each axis
+  const int l0x = v0x - b0x * MH_BLOCK_SIDE, l1x = v1x - (b0x + ex) * MH_BLOCK_SIDE;
+  const int l0y = v0y - b0y * MH_BLOCK_SIDE, l1y = v1y - (b0y + ey) * MH_BLOCK_SIDE;
+  const int l0z = v0z - b0z * MH_BLOCK_SIDE, l1z = v1z - (b0z + ez) * MH_BLOCK_SIDE;
   float s = 0.0f;
-  if (lx < MH_BLOCK_SIDE - 1 && ly < MH_BLOCK_SIDE - 1 && lz < MH_BLOCK_SIDE - 1 && v1x == v0x + 1 &&
-      v1y == v0y + 1 && v1z == v0z + 1) {
-    const float *base = d.sdf + (size_t)c.ptr * MH_BLOCK_VOXELS + lx + ly * 8 + lz * 64;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int mx = (i & 4) > 0, my = (i & 2) > 0, mz = (i & 1) > 0;
-      const float w = (mx ? rx : w0x) * (my ? ry : w0y) * (mz ? rz : w0z);
-      s += w * __ldg(base + mx + my * 8 + mz * 64);
-    }
-  } else {
-#pragma unroll 1
-    for (int i = 0; i < 8; ++i) {
-      const int mx = (i & 4) > 0, my = (i & 2) > 0, mz = (i & 1) > 0;
-      const int vx = mx ? v1x : v0x, vy = my ? v1y : v0y, vz = mz ? v1z : v0z;
-      const float w = (mx ? rx : w0x) * (my ? ry : w0y) * (mz ? rz : w0z);
-      const int bx = vox2blk(vx), by = vox2blk(vy), bz = vox2blk(vz);
-      int ptr = c.ptr;
-      if (bx != b0x || by != b0y || bz != b0z) {
-        if (bx != c.ox || by != c.oy || bz != c.oz) {
-          c.ox = bx, c.oy = by, c.oz = bz;
-          c.optr = hash_find(d, bx, by, bz);
-        }
-        ptr = c.optr;
-        if (ptr < 0) return RS_MISS;
-      }
-      const int li = (vx - bx * MH_BLOCK_SIDE) + (vy - by * MH_BLOCK_SIDE) * MH_BLOCK_SIDE +
-                     (vz - bz * MH_BLOCK_SIDE) * MH_BLOCK_SIDE * MH_BLOCK_SIDE;
-      s += w * __ldg(d.sdf + (size_t)ptr * MH_BLOCK_VOXELS + li);
-    }
+  for (int i = 0; i < 8; ++i) {
+    const int mx = (i & 4) > 0, my = (i & 2) > 0, mz = (i & 1) > 0;
+    const float w = (mx ? rx : w0x) * (my ? ry : w0y) * (mz ? rz : w0z);
+    const int n = (mx & ex) | ((my & ey) << 1) | ((mz & ez) << 2);
+    const int li = (mx ? l1x : l0x) + (my ? l1y : l0y) * MH_BLOCK_SIDE +
+                   (mz ? l1z : l0z) * MH_BLOCK_SIDE * MH_BLOCK_SIDE;
+    s += w * __ldg(d.sdf + (size_t)c.p[n] * MH_BLOCK_VOXELS + li);
   }
   sdf = s;
   return RS_OK;
