@@ -107,15 +107,10 @@ __global__ void __launch_bounds__(128) k_integrate_simple(Dev d) {
   }
 }
 
-// gaussian() of geometry/geometry_helper.h:30-34 (no 1/2 in the exponent)
-__device__ __forceinline__ float gaussianf(float x, float u, float s2) {
-  return 1.0f / (2.50662827463100050f * sqrtf(s2)) * expf(-((x - u) * (x - u)) / s2);
-}
-
-// UpdateBlocksBayesianKernel (mapping/update_bayesian.cu:103-185).  The
-// variance update uses C1 s^2 + C2 sigma^2 + C1 C2 (m - mu)^2, algebraically
-// equal to the reference's C1(s^2+m^2) + C2(sigma^2+mu^2) - sdf'^2 when
-// C1 + C2 = 1, but free of its single-precision cancellation.
+// UpdateBlocksBayesianKernel (mapping/update_bayesian.cu:103-185).  Per voxel
+// the update is division- and transcendental-bound, not load-bound, so the
+// default form regroups it to 10 IEEE divisions (see below); compat mode
+// evaluates the reference's expressions as written.
 __global__ void __launch_bounds__(128) k_integrate_psdf(Dev d) {
   __shared__ float cTw[16];
   if (threadIdx.x < 16) cTw[threadIdx.x] = d.fc->cTw[threadIdx.x];
@@ -166,34 +161,65 @@ __global__ void __launch_bounds__(128) k_integrate_psdf(Dev d) {
         continue;
       }
       const float mu = get(S, k);
-      const float s2 = 1.0f / w0;
+      const float a = get(A, k), b = get(B, k);
       const float t2 = tau * tau;
-      const float ss2 = 1.0f / (1.0f / s2 + 1.0f / t2);
-      const float m = ss2 * (mu / s2 + x / t2);
-      float C1;
+      const bool in_range = dd < p.max_depth_range && dd >= p.min_depth_range;
       if (p.compat) {
-        // as the reference evaluates it: sqrt(2 pi) in double, so the product
-        // and the reciprocal are double (geometry_helper.h:30-34)
+        // the reference's expressions as written (update_bayesian.cu:140-180);
+        // sqrt(2 pi) is a double there, so the product and the reciprocal of
+        // gaussian() are double (geometry_helper.h:30-34)
+        const float s2 = 1.0f / w0;
+        const float ss2 = 1.0f / (1.0f / s2 + 1.0f / t2);
+        const float m = ss2 * (mu / s2 + x / t2);
         const float sv = s2 + t2;
         const double g = 1.0 / (2.5066282746310002 * (double)sqrtf(sv)) * (double)expf(-((x - mu) * (x - mu)) / sv);
-        C1 = (float)((double)r * g);
-      } else {
-        C1 = r * gaussianf(x, mu, s2 + t2);
+        float C1 = (float)((double)r * g);
+        float C2 = in_range ? (1.0f - r) * 1.0f / (5.0f - 0.1f) : 1.0f;
+        const float sum = C1 + C2;
+        C1 /= sum;
+        C2 /= sum;
+        const float f = C1 * (a + 1) / (a + b + 1) + C2 * a / (a + b + 1);
+        const float e =
+            C1 * (a + 1) * (a + 2) / ((a + b + 1) * (a + b + 2)) + C2 * a * (a + 1) / ((a + b + 1) * (a + b + 2));
+        const float nsdf = C1 * m + C2 * mu;
+        const float var = C1 * (ss2 + m * m) + C2 * (s2 + mu * mu) - nsdf * nsdf;
+        put(S, k, nsdf);
+        put(W, k, 1.0f / var);
+        const float na = (e - f) / (f - e / f);
+        put(A, k, na);
+        put(B, k, na * (1.0f - f) / f);
+        continue;
       }
-      float C2 = (dd < p.max_depth_range && dd >= p.min_depth_range) ? (1.0f - r) * 1.0f / (5.0f - 0.1f) : 1.0f;
-      const float sum = C1 + C2;
-      C1 /= sum;
-      C2 /= sum;
-      const float a = get(A, k), b = get(B, k);
-      const float f = C1 * (a + 1) / (a + b + 1) + C2 * a / (a + b + 1);
-      const float e = C1 * (a + 1) * (a + 2) / ((a + b + 1) * (a + b + 2)) + C2 * a * (a + 1) / ((a + b + 1) * (a + b + 2));
+      // The same update with 10 divisions instead of 21: 1/s2 is the stored
+      // weight itself, reciprocals are shared, f and e are put over common
+      // denominators, (e - f) / (f - e/f) is taken as f (e - f) / (f^2 - e),
+      // and the variance is C1 s^2 + C2 sigma^2 + C1 C2 (m - mu)^2, equal to
+      // the reference's C1 (s^2 + m^2) + C2 (sigma^2 + mu^2) - sdf'^2 when
+      // C1 + C2 = 1 but free of its cancellation.
+      const float s2 = 1.0f / w0;
+      const float it2 = 1.0f / t2;
+      const float ss2 = 1.0f / (w0 + it2);
+      const float m = ss2 * (mu * w0 + x * it2);
+      const float sv = s2 + t2;
+      const float isv = 1.0f / sv;
+      const float dx = x - mu;
+      // gaussian(): exp(-dx^2 / sv) / sqrt(2 pi sv)
+      const float g = expf(-(dx * dx) * isv) * (sqrtf(sv) * isv) * 0.398942280401432678f;
+      float C1 = r * g;
+      float C2 = in_range ? (1.0f - r) * 0.204081632653061224f : 1.0f;
+      const float isum = 1.0f / (C1 + C2);
+      C1 *= isum;
+      C2 *= isum;
+      const float ab1 = a + b + 1.0f;
+      const float iab1 = 1.0f / ab1;
+      const float f = (C1 * (a + 1.0f) + C2 * a) * iab1;
+      const float e = (a + 1.0f) * (C1 * (a + 2.0f) + C2 * a) * iab1 / (ab1 + 1.0f);
       const float nsdf = C1 * m + C2 * mu;
       const float dm = m - mu;
-      const float var = p.compat ? C1 * (ss2 + m * m) + C2 * (s2 + mu * mu) - nsdf * nsdf
-                                 : C1 * ss2 + C2 * s2 + C1 * C2 * (dm * dm);
+      const float var = C1 * ss2 + C2 * s2 + C1 * C2 * (dm * dm);
       put(S, k, nsdf);
       put(W, k, 1.0f / var);
-      const float na = (e - f) / (f - e / f);
+      const float na = f * (e - f) / (f * f - e);
       put(A, k, na);
       put(B, k, na * (1.0f - f) / f);
     }
@@ -300,19 +326,19 @@ __global__ void k_preprocess(Dev d, const float *src, const uint16_t *src16, flo
 static int grid_persistent(int per_sm) { return mh_sm_count() * per_sm; }
 
 int launch_integrate_simple(const Dev &d, cudaStream_t s) {
-  k_integrate_simple<<<grid_persistent(12), 128, 0, s>>>(d);
+  k_integrate_simple<<<mh_resident_grid((const void *)k_integrate_simple, 128, 16), 128, 0, s>>>(d);
   mh_count_launches(1);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }
 int launch_integrate_psdf(const Dev &d, cudaStream_t s) {
-  k_integrate_psdf<<<grid_persistent(12), 128, 0, s>>>(d);
+  k_integrate_psdf<<<mh_resident_grid((const void *)k_integrate_psdf, 128, 16), 128, 0, s>>>(d);
   mh_count_launches(1);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }
 int launch_predict_inlier(const Dev &d, cudaStream_t s) {
   MH_CUDA_TRY(cudaMemsetAsync(&d.ctr->vtx_list_count, 0, sizeof(int), s));
   k_vtx_select<<<grid_persistent(4), 256, 0, s>>>(d);
-  k_predict_inlier<<<grid_persistent(12), 128, 0, s>>>(d);
+  k_predict_inlier<<<mh_resident_grid((const void *)k_predict_inlier, 128, 16), 128, 0, s>>>(d);
   mh_count_launches(2);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }

@@ -414,5 +414,7 @@ __device__ __forceinline__ void release_page_cta(const Dev &d, int blk, int pg) 
   } while (0)
 
 int mh_sm_count();
+// CTAs of a persistent grid: resident CTAs per SM (at most cap_per_sm) x SMs
+int mh_resident_grid(const void *fn, int block, int cap_per_sm);
 // every launcher adds the kernels it launched (reported by mh_launch_count)
 void mh_count_launches(int n);

@@ -7,10 +7,12 @@
 // mh_volume owns all device state, stages are asynchronous on the caller's
 // stream, and counts stay in device memory; only the introspection calls
 // synchronise.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <unordered_map>
 #include <vector>
 
@@ -74,6 +76,26 @@ int mh_sm_count() {
     if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 132;
   }
   return n;
+}
+
+// Persistent grids: as many CTAs as can be resident at once (at most
+// cap_per_sm per SM), so that a grid-stride loop never leaves a second,
+// partly filled wave of CTAs behind the first.
+int mh_resident_grid(const void *fn, int block, int cap_per_sm) {
+  static std::mutex mu;
+  static std::unordered_map<const void *, int> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(fn);
+  int per_sm;
+  if (it != cache.end()) {
+    per_sm = it->second;
+  } else {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, 0) != cudaSuccess || n <= 0) n = 1;
+    per_sm = n;
+    cache[fn] = n;
+  }
+  return std::min(per_sm, cap_per_sm) * mh_sm_count();
 }
 
 // ------------------------------------------------------------------ helpers

@@ -636,12 +636,50 @@ template <class R> struct Vol {
           continue;
         }
         R mu = b->sdf[i];
-        R s2 = (R)1 / b->w[i];
+        R a = b->a[i], bb = b->b[i];
         R t2 = tau * tau;
+        const bool in_range = d < (R)p.max_depth_range && d >= (R)p.min_depth_range;
+        if (sizeof(R) == 4 && !p.compat_arithmetic) {
+          // the single-precision form of the library: 10 divisions, same
+          // operation order (1/s2 is the stored weight, shared reciprocals,
+          // f and e over common denominators, f (e - f) / (f^2 - e), and the
+          // variance as C1 s^2 + C2 sigma^2 + C1 C2 (m - mu)^2)
+          const float w0 = (float)b->w[i], muf = (float)mu, xf = (float)x, rf = (float)rho, t2f = (float)t2;
+          const float af = (float)a, bf = (float)bb;
+          const float s2 = 1.0f / w0;
+          const float it2 = 1.0f / t2f;
+          const float ss2 = 1.0f / (w0 + it2);
+          const float m = ss2 * (muf * w0 + xf * it2);
+          const float sv = s2 + t2f;
+          const float isv = 1.0f / sv;
+          const float dx = xf - muf;
+          const float g = std::exp(-(dx * dx) * isv) * (std::sqrt(sv) * isv) * 0.398942280401432678f;
+          float C1 = rf * g;
+          float C2 = in_range ? (1.0f - rf) * 0.204081632653061224f : 1.0f;
+          const float isum = 1.0f / (C1 + C2);
+          C1 *= isum;
+          C2 *= isum;
+          const float ab1 = af + bf + 1.0f;
+          const float iab1 = 1.0f / ab1;
+          const float f = (C1 * (af + 1.0f) + C2 * af) * iab1;
+          const float e = (af + 1.0f) * (C1 * (af + 2.0f) + C2 * af) * iab1 / (ab1 + 1.0f);
+          const float nsdf = C1 * m + C2 * muf;
+          const float dm = m - muf;
+          const float var = C1 * ss2 + C2 * s2 + C1 * C2 * (dm * dm);
+          const float na = f * (e - f) / (f * f - e);
+          b->sdf[i] = nsdf;
+          b->w[i] = 1.0f / var;
+          b->a[i] = na;
+          b->b[i] = na * (1.0f - f) / f;
+          continue;
+        }
+        // the reference's expressions (update_bayesian.cu:140-180): in double
+        // for the FP64 oracle, in float with its double gaussian() in compat
+        R s2 = (R)1 / b->w[i];
         R ss2 = (R)1 / ((R)1 / s2 + (R)1 / t2);
         R m = ss2 * (mu / s2 + x / t2);
         R C1;
-        if (sizeof(R) == 4 && p.compat_arithmetic) {
+        if (sizeof(R) == 4) {
           // the reference's promotion: sqrt(2 pi) is a double (geometry_helper.h:30-34)
           const float sv = (float)(s2 + t2);
           const double g = 1.0 / (2.5066282746310002 * (double)std::sqrt(sv)) *
@@ -650,22 +688,14 @@ template <class R> struct Vol {
         } else {
           C1 = rho * gaussian(x, mu, s2 + t2);
         }
-        R C2 = (d < (R)p.max_depth_range && d >= (R)p.min_depth_range) ? ((R)1 - rho) * (R)1 / ((R)5 - (R)0.1f)
-                                                                         : (R)1;
+        R C2 = in_range ? ((R)1 - rho) * (R)1 / ((R)5 - (R)0.1f) : (R)1;
         R sum = C1 + C2;
         C1 /= sum;
         C2 /= sum;
-        R a = b->a[i], bb = b->b[i];
         R f = C1 * (a + 1) / (a + bb + 1) + C2 * a / (a + bb + 1);
         R e = C1 * (a + 1) * (a + 2) / ((a + bb + 1) * (a + bb + 2)) + C2 * a * (a + 1) / ((a + bb + 1) * (a + bb + 2));
         R nsdf = C1 * m + C2 * mu;
-        R var;
-        if (sizeof(R) == 8 || p.compat_arithmetic) {
-          var = C1 * (ss2 + m * m) + C2 * (s2 + mu * mu) - nsdf * nsdf;
-        } else {
-          R dm = m - mu;
-          var = C1 * ss2 + C2 * s2 + C1 * C2 * (dm * dm);
-        }
+        R var = C1 * (ss2 + m * m) + C2 * (s2 + mu * mu) - nsdf * nsdf;
         b->sdf[i] = nsdf;
         b->w[i] = (R)1 / var;
         R na = (e - f) / (f - e / f);

@@ -136,6 +136,53 @@ def test_oracle_fp32_close_to_fp64(built):
     assert rel_w.max() < 1e-5
 
 
+def test_oracle_psdf_fp32_close_to_fp64(built):
+    """One PSDF update from the same state and inlier image in each precision:
+    the single-precision form (10 divisions, regrouped) against the
+    reference's expressions evaluated in double.  Weights and the inlier
+    Beta parameters within 1e-5 relative; sdf within 2e-6 m absolute, the
+    rounding of a single-precision camera depth of a few metres, which both
+    forms share (a relative bound is meaningless at the zero crossing)."""
+    wl = scene.full_spline(40, width=160, height=120)
+    p = config.params_for(wl, value_capacity=1 << 16)
+    o32 = O.Oracle(p, fp64=False)
+    for i in range(6):
+        o32.frame_set(wl.frame(i), wl.pose(i))
+        o32.allocate()
+        o32.collect_frustum()
+        o32.predict_inlier()
+        o32.integrate_psdf()
+        o32.mesh()
+    d, T = wl.frame(6), wl.pose(6)
+    o32.frame_set(d, T)
+    o32.allocate()
+    o32.collect_frustum()
+    o32.predict_inlier()
+    pos, s, w, a, b = o32.blocks()
+    o64 = O.Oracle(p, fp64=True)
+    o64.set_blocks(pos, s, w, a, b)
+    o64.frame_set(d, T)
+    o64.set_inlier(o32.inlier())
+    o64.set_candidates(o32.candidates())
+    o32.integrate_psdf()
+    o64.integrate_psdf()
+    p32, s32, w32, a32, b32 = o32.blocks()
+    p64, s64, w64, a64, b64 = o64.blocks()
+    from tests._util import align
+    g, o = [x.reshape(-1) for x in align(p32, s32, p64, s64)[:2]]
+    gw, ow = [x.reshape(-1) for x in align(p32, w32, p64, w64)[:2]]
+    ga, oa = [x.reshape(-1) for x in align(p32, a32, p64, a64)[:2]]
+    gb, ob = [x.reshape(-1) for x in align(p32, b32, p64, b64)[:2]]
+    _, w_before = [x.reshape(-1) for x in align(p32, w32, pos, w)[:2]]
+    upd = ow > 0
+    later = upd & (w_before > 0)          # voxels that went through the Bayesian update
+    assert later.sum() > 100000
+    assert np.abs(g - o)[upd].max() < 2e-6
+    assert (np.abs(gw - ow)[upd] / ow[upd]).max() < 1e-5
+    assert (np.abs(ga - oa)[later] / np.abs(oa[later])).max() < 1e-5
+    assert (np.abs(gb - ob)[later] / np.abs(ob[later])).max() < 1e-5
+
+
 def test_oracle_raycast_hits_the_scene(built):
     wl, p, o = _run_oracle(True, n_frames=6)
     i = 25
