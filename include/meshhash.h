@@ -256,6 +256,52 @@ int mh_profile_read(mh_volume *v, double ms[MH_STAGE_COUNT], int calls[MH_STAGE_
 uint64_t mh_launch_count(void);
 
 /* Teschner hash of a block position (core/hash_table.h:259-269). */
+/* ------------------------------------------------------------------ batches
+ * Many independent volumes (scenes) advanced together.  No reference
+ * counterpart: the reference runs one MainEngine per process.  A step runs
+ * one MainEngine frame (the mh_integrate_frame chain) for every active scene,
+ * with ONE launch per stage for all scenes: the batched kernels walk a device
+ * scene table and share the single-scene kernels' code, so each scene's
+ * results are those of mh_integrate_frame on the same inputs.  Scenes may
+ * differ in resolution, voxel size and update mode.  With use_graph the whole
+ * step (table upload, depth upload, every stage) is captured once as a CUDA
+ * graph and replayed; the per-step inputs travel in a double-buffered pinned
+ * block, so a replay needs no re-capture.  While a volume belongs to a batch,
+ * its standalone stage calls need mh_frame_set first (the batch keeps the
+ * scenes' poses in its own device table).
+ */
+typedef struct mh_batch mh_batch;
+
+typedef struct mh_batch_tuning {
+  int ray_tile_shape;        /* raycast CTA tile: 0 = 16x8, 1 = 8x8, 2 = 32x4 */
+  int integrate_cta_per_sm;  /* cap on resident CTAs per SM of the integrate grid */
+} mh_batch_tuning;
+
+/* Build a batch over `count` volumes (the caller keeps ownership and must
+ * destroy the batch first).  raycast != 0 allocates per-scene raycast outputs
+ * (depth W x H float, vertex and normal W x H float4) written every step. */
+int mh_batch_create(mh_volume *const *volumes, int count, int raycast, mh_batch **out);
+int mh_batch_destroy(mh_batch *b);
+/* One frame for every scene s with active[s] != 0 (active == NULL: all):
+ * depth[s] is W_s x H_s metres (device pointers if depth_on_device, else host),
+ * wTc is count x 16 row-major camera-to-world poses (host). */
+int mh_batch_step(mh_batch *b, const float *const *depth, int depth_on_device, const float *wTc,
+                  const int *active, int tv_iterations, float tv_lambda, int use_graph, void *stream);
+/* device pointers of scene s's raycast outputs (NULL where not allocated) */
+int mh_batch_outputs(mh_batch *b, int scene, float **depth, float **vertex4, float **normal4);
+/* copy scene s's last raycast outputs to host buffers (NULL: skipped; synchronising) */
+int mh_batch_dump_raycast(mh_batch *b, int scene, float *depth, float *vertex4, float *normal4);
+int mh_batch_get_tuning(mh_batch *b, mh_batch_tuning *out);
+int mh_batch_set_tuning(mh_batch *b, const mh_batch_tuning *t);
+/* Online autotuning: the next (raycast tile shapes x integrate CTA caps x
+ * trials) steps each run one combination, timed with CUDA events around the
+ * two stages it affects; then the fastest choice per stage is kept.  The
+ * steps do their normal work (launch shapes do not change results). */
+int mh_batch_autotune(mh_batch *b, int trials);
+/* ms per step of the integrate and raycast stages measured by the autotuner
+ * for each choice (3 shapes, 3 caps), -1 where not measured */
+int mh_batch_tuning_times(mh_batch *b, double ray_ms[3], double integrate_ms[3]);
+
 uint32_t mh_hash_bucket(int32_t x, int32_t y, int32_t z, uint32_t bucket_count);
 /* Bytes the last frame's stages needed by the algorithmic model (see the
  * design notes); per stage: [alloc, collect, integrate, predict, mesh, raycast]. */

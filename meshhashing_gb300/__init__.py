@@ -7,3 +7,4 @@ as hand-written sm_103a CUDA kernels behind the C ABI in include/meshhash.h.
 from ._abi import MhParams, MhStats, STATUS_NAMES  # noqa: F401
 from ._lib import MeshHashError, load  # noqa: F401
 from .volume import Volume, default_params, hash_bucket, launch_count  # noqa: F401
+from .batch import Batch  # noqa: F401

@@ -40,3 +40,8 @@ class MhStats(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class MhBatchTuning(C.Structure):
+    """mh_batch_tuning (include/meshhash.h)."""
+    _fields_ = [("ray_tile_shape", C.c_int32), ("integrate_cta_per_sm", C.c_int32)]

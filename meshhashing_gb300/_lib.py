@@ -9,7 +9,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-from ._abi import MhParams, MhStats
+from ._abi import MhBatchTuning, MhParams, MhStats
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmeshhash.so")
@@ -61,6 +61,15 @@ SIGNATURES = {
     "mh_profile_read": (i32, [MHV, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "mh_launch_count": (C.c_uint64, []),
     "mh_denoise_tv_static": (i32, [vp, vp, i32, i32, C.c_float, i32, vp]),
+    "mh_batch_create": (i32, [C.POINTER(MHV), i32, i32, C.POINTER(vp)]),
+    "mh_batch_destroy": (i32, [vp]),
+    "mh_batch_step": (i32, [vp, C.POINTER(vp), i32, f32p, i32p, i32, C.c_float, i32, vp]),
+    "mh_batch_outputs": (i32, [vp, i32, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
+    "mh_batch_dump_raycast": (i32, [vp, i32, f32p, f32p, f32p]),
+    "mh_batch_get_tuning": (i32, [vp, C.POINTER(MhBatchTuning)]),
+    "mh_batch_set_tuning": (i32, [vp, C.POINTER(MhBatchTuning)]),
+    "mh_batch_autotune": (i32, [vp, i32]),
+    "mh_batch_tuning_times": (i32, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 }
 SYMBOLS = sorted(SIGNATURES)
 

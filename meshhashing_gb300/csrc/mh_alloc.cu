@@ -14,13 +14,16 @@
 #include "mh_internal.cuh"
 #include "mh_hash.cuh"
 #include "mh_kernels.h"
+#include "mh_batch.cuh"
+
+#include <algorithm>
 
 // ------------------------------------------------------------------ alloc
 
 #define ALLOC_TILE 16
 #define ALLOC_SET 1024
 
-__global__ void __launch_bounds__(ALLOC_TILE * ALLOC_TILE) k_alloc(Dev d) {
+__device__ __forceinline__ void alloc_body(const Dev &d, int tile_x, int tile_y) {
   __shared__ unsigned long long set[ALLOC_SET];
   __shared__ float sm[32];
   const int tid = threadIdx.x + threadIdx.y * ALLOC_TILE;
@@ -30,8 +33,8 @@ __global__ void __launch_bounds__(ALLOC_TILE * ALLOC_TILE) k_alloc(Dev d) {
   __syncthreads();
   const float *wTc = sm, *cTw = sm + 16;
   const DevParams &p = d.p;
-  const unsigned x = blockIdx.x * ALLOC_TILE + threadIdx.x;
-  const unsigned y = blockIdx.y * ALLOC_TILE + threadIdx.y;
+  const unsigned x = tile_x * ALLOC_TILE + threadIdx.x;
+  const unsigned y = tile_y * ALLOC_TILE + threadIdx.y;
   const float vs = p.voxel_size;
 
   if (x < p.width && y < p.height) {
@@ -107,13 +110,20 @@ __global__ void __launch_bounds__(ALLOC_TILE * ALLOC_TILE) k_alloc(Dev d) {
     hash_insert(d, bx, by, bz);
   }
 }
+__global__ void __launch_bounds__(ALLOC_TILE * ALLOC_TILE) k_alloc(Dev d) { alloc_body(d, blockIdx.x, blockIdx.y); }
+__global__ void __launch_bounds__(ALLOC_TILE * ALLOC_TILE) k_alloc_b(const Scene *t, int n, int total) {
+  each_tile(t, n, total, &Scene::alloc_tile0, [&](const Scene &c, int lt) {
+    const int tw = (c.d.p.width + ALLOC_TILE - 1) / ALLOC_TILE;
+    alloc_body(c.d, lt % tw, lt / tw);
+  });
+}
 
 // ------------------------------------------------------------------ collect
 // CollectBlocksInFrustumKernel / CollectAllBlocksKernel
 // (core/collect_block_array.cu:25-91), over the block pool's live indices
 // [0, high_water) instead of all hash entries; warp-ballot compaction with one
 // atomic per warp.
-__global__ void __launch_bounds__(256) k_collect(Dev d, int frustum) {
+__device__ __forceinline__ void collect_body(const Dev &d, int frustum) {
   __shared__ float cTw[16];
   if (threadIdx.x < 16) cTw[threadIdx.x] = d.fc->cTw[threadIdx.x];
   __syncthreads();
@@ -133,6 +143,10 @@ __global__ void __launch_bounds__(256) k_collect(Dev d, int frustum) {
     slot = __shfl_sync(0xffffffffu, slot, 0);
     if (keep) d.cand[slot + __popc(m & lanemask_lt())] = make_int4(bp.x, bp.y, bp.z, i);
   }
+}
+__global__ void __launch_bounds__(256) k_collect(Dev d, int frustum) { collect_body(d, frustum); }
+__global__ void __launch_bounds__(256) k_collect_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { collect_body(c.d, 1); });
 }
 
 // Insert host-given blocks (state loading) and report their indices.
@@ -182,6 +196,19 @@ int launch_find_list(const Dev &d, const int *pos_dev, int n, int *ptr_dev, cuda
 }
 int launch_set_candidates(const Dev &d, const int *pos_dev, const int *ptr_dev, int n, cudaStream_t s) {
   k_set_candidates<<<(max(n, 1) + 127) / 128, 128, 0, s>>>(d, pos_dev, ptr_dev, n);
+  mh_count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+
+// ------------------------------------------------------------------ batched
+int launch_batch_alloc(const Scene *t, int n, int total_tiles, cudaStream_t s) {
+  const int grid = std::max(1, std::min(total_tiles, mh_sm_count() * 8));
+  k_alloc_b<<<grid, dim3(ALLOC_TILE, ALLOC_TILE), 0, s>>>(t, n, total_tiles);
+  mh_count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+int launch_batch_collect(const Scene *t, int n, cudaStream_t s) {
+  k_collect_b<<<mh_sm_count() * 4, 256, 0, s>>>(t, n);
   mh_count_launches(1);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }

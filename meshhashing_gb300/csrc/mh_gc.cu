@@ -11,10 +11,13 @@
 #include "mh_internal.cuh"
 #include "mh_hash.cuh"
 #include "mh_kernels.h"
+#include "mh_batch.cuh"
+
+#include <algorithm>
 
 
 // CollectLowSurfelBlocksKernel, first half (recycle.cu:91-99)
-__global__ void k_gc_life(Dev d) {
+__device__ __forceinline__ void gc_life_body(const Dev &d) {
   const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
     d.flags[c] = 0;
@@ -24,9 +27,13 @@ __global__ void k_gc_life(Dev d) {
     else d.life[ptr] = MH_BLOCK_LIFE;
   }
 }
+__global__ void k_gc_life(Dev d) { gc_life_body(d); }
+__global__ void k_gc_life_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { gc_life_body(c.d); });
+}
 
 // CollectLowSurfelBlocksKernel, second half (recycle.cu:102-113)
-__global__ void k_gc_flag(Dev d) {
+__device__ __forceinline__ void gc_flag_body(const Dev &d) {
   const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
   const int off[6][3] = {{0, 0, 1}, {0, 0, -1}, {0, 1, 0}, {0, -1, 0}, {1, 0, 0}, {-1, 0, 0}};
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
@@ -40,9 +47,13 @@ __global__ void k_gc_flag(Dev d) {
     if (ok) d.flags[c] = 1;
   }
 }
+__global__ void k_gc_flag(Dev d) { gc_flag_body(d); }
+__global__ void k_gc_flag_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { gc_flag_body(c.d); });
+}
 
 // StarveOccupiedBlocksKernel (recycle.cu:15-25)
-__global__ void __launch_bounds__(128) k_gc_starve(Dev d) {
+__device__ __forceinline__ void gc_starve_body(const Dev &d) {
   const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
     const int ptr = d.cand[c].w;
@@ -54,9 +65,13 @@ __global__ void __launch_bounds__(128) k_gc_starve(Dev d) {
     *w4 = w;
   }
 }
+__global__ void __launch_bounds__(128) k_gc_starve(Dev d) { gc_starve_body(d); }
+__global__ void __launch_bounds__(128) k_gc_starve_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { if (c.starve) gc_starve_body(c.d); });
+}
 
 // CollectGarbageBlockArrayKernel (recycle.cu:28-75)
-__global__ void __launch_bounds__(128) k_gc_garbage(Dev d) {
+__device__ __forceinline__ void gc_garbage_body(const Dev &d) {
   __shared__ float smin[4], smax[4];
   const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
   const float inf = __int_as_float(0x7f800000);
@@ -92,9 +107,13 @@ __global__ void __launch_bounds__(128) k_gc_garbage(Dev d) {
     __syncthreads();
   }
 }
+__global__ void __launch_bounds__(128) k_gc_garbage(Dev d) { gc_garbage_body(d); }
+__global__ void __launch_bounds__(128) k_gc_garbage_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { if (c.starve) gc_garbage_body(c.d); });
+}
 
 // RecycleGarbageTrianglesKernel (recycle.cu:117-142)
-__global__ void __launch_bounds__(128) k_gc_recycle_tri(Dev d) {
+__device__ __forceinline__ void gc_recycle_tri_body(const Dev &d) {
   const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
     const int ptr = d.cand[c].w;
@@ -115,9 +134,13 @@ __global__ void __launch_bounds__(128) k_gc_recycle_tri(Dev d) {
     }
   }
 }
+__global__ void __launch_bounds__(128) k_gc_recycle_tri(Dev d) { gc_recycle_tri_body(d); }
+__global__ void __launch_bounds__(128) k_gc_recycle_tri_b(const Scene *t, int n, int which) {
+  each_scene(t, n, [&](const Scene &c) { if (which ? c.starve : c.recycle) gc_recycle_tri_body(c.d); });
+}
 
 // RecycleGarbageVerticesKernel (recycle.cu:144-181) + FreeEntry + Block::Clear
-__global__ void __launch_bounds__(128) k_gc_recycle_vtx(Dev d) {
+__device__ __forceinline__ void gc_recycle_vtx_body(const Dev &d) {
   __shared__ int live;
   const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
@@ -171,6 +194,10 @@ __global__ void __launch_bounds__(128) k_gc_recycle_vtx(Dev d) {
     if (threadIdx.x == 0) stack_push(&d.ctr->heap_top, d.heap, ptr);
   }
 }
+__global__ void __launch_bounds__(128) k_gc_recycle_vtx(Dev d) { gc_recycle_vtx_body(d); }
+__global__ void __launch_bounds__(128) k_gc_recycle_vtx_b(const Scene *t, int n, int which) {
+  each_scene(t, n, [&](const Scene &c) { if (which ? c.starve : c.recycle) gc_recycle_vtx_body(c.d); });
+}
 
 int launch_gc_low_surfel(const Dev &d, cudaStream_t s) {
   const int g = mh_sm_count() * 2;
@@ -193,6 +220,29 @@ int launch_gc_recycle(const Dev &d, cudaStream_t s) {
   const int g = mh_sm_count() * 8;
   k_gc_recycle_tri<<<g, 128, 0, s>>>(d);
   k_gc_recycle_vtx<<<g, 128, 0, s>>>(d);
+  mh_count_launches(2);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+
+// ------------------------------------------------------------------ batched
+int launch_batch_gc_low_surfel(const Scene *t, int n, cudaStream_t s) {
+  const int g = mh_sm_count() * 2;
+  k_gc_life_b<<<g, 256, 0, s>>>(t, n);
+  k_gc_flag_b<<<g, 256, 0, s>>>(t, n);
+  mh_count_launches(2);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+// which = 0: scenes due for the periodic recycle; 1: scenes due for starvation
+int launch_batch_gc_recycle(const Scene *t, int n, int which, cudaStream_t s) {
+  const int g = mh_sm_count() * 8;
+  k_gc_recycle_tri_b<<<g, 128, 0, s>>>(t, n, which);
+  k_gc_recycle_vtx_b<<<g, 128, 0, s>>>(t, n, which);
+  mh_count_launches(2);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+int launch_batch_gc_starve(const Scene *t, int n, cudaStream_t s) {
+  k_gc_starve_b<<<mh_sm_count() * 8, 128, 0, s>>>(t, n);
+  k_gc_garbage_b<<<mh_sm_count() * 8, 128, 0, s>>>(t, n);
   mh_count_launches(2);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }

@@ -10,6 +10,7 @@
 // depth pixel inside the truncation band.
 #include "mh_internal.cuh"
 #include "mh_kernels.h"
+#include "mh_batch.cuh"
 
 namespace {
 
@@ -56,7 +57,7 @@ __device__ __forceinline__ void note_wmax(const Dev &d, int blk, float w) {
 }  // namespace
 
 // UpdateBlocksSimpleKernel + Voxel::Update (core/voxel.h:107-115)
-__global__ void __launch_bounds__(128) k_integrate_simple(Dev d) {
+__device__ __forceinline__ void integrate_simple_body(const Dev &d) {
   __shared__ float cTw[16];
   if (threadIdx.x < 16) cTw[threadIdx.x] = d.fc->cTw[threadIdx.x];
   __syncthreads();
@@ -106,12 +107,16 @@ __global__ void __launch_bounds__(128) k_integrate_simple(Dev d) {
     note_wmax(d, cb.w, fmaxf(fmaxf(W.x, W.y), fmaxf(W.z, W.w)));
   }
 }
+__global__ void __launch_bounds__(128) k_integrate_simple(Dev d) { integrate_simple_body(d); }
+__global__ void __launch_bounds__(128) k_integrate_simple_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { if (!c.d.p.enable_bayesian) integrate_simple_body(c.d); });
+}
 
 // UpdateBlocksBayesianKernel (mapping/update_bayesian.cu:103-185).  Per voxel
 // the update is division- and transcendental-bound, not load-bound, so the
 // default form regroups it to 10 IEEE divisions (see below); compat mode
 // evaluates the reference's expressions as written.
-__global__ void __launch_bounds__(128) k_integrate_psdf(Dev d) {
+__device__ __forceinline__ void integrate_psdf_body(const Dev &d) {
   __shared__ float cTw[16];
   if (threadIdx.x < 16) cTw[threadIdx.x] = d.fc->cTw[threadIdx.x];
   __syncthreads();
@@ -230,13 +235,17 @@ __global__ void __launch_bounds__(128) k_integrate_psdf(Dev d) {
     note_wmax(d, cb.w, fmaxf(fmaxf(W.x, W.y), fmaxf(W.z, W.w)));
   }
 }
+__global__ void __launch_bounds__(128) k_integrate_psdf(Dev d) { integrate_psdf_body(d); }
+__global__ void __launch_bounds__(128) k_integrate_psdf_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { if (c.d.p.enable_bayesian) integrate_psdf_body(c.d); });
+}
 
 // PredictOutlierRatioKernel (mapping/update_bayesian.cu:36-101).  The
 // per-pixel float max uses an integer atomicMax on the bit pattern, exact for
 // the positive ratios involved (all >= 0.01).  Blocks that own no vertex are
 // skipped.  The vertex normal is transformed by cTw as a point (with the
 // translation), as the reference does (update_bayesian.cu:83-86).
-__global__ void __launch_bounds__(128) k_predict_inlier(Dev d) {
+__device__ __forceinline__ void predict_inlier_body(const Dev &d) {
   __shared__ float cTw[16];
   if (threadIdx.x < 16) cTw[threadIdx.x] = d.fc->cTw[threadIdx.x];
   __syncthreads();
@@ -290,10 +299,14 @@ __global__ void __launch_bounds__(128) k_predict_inlier(Dev d) {
     }
   }
 }
+__global__ void __launch_bounds__(128) k_predict_inlier(Dev d) { predict_inlier_body(d); }
+__global__ void __launch_bounds__(128) k_predict_inlier_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { if (c.d.p.enable_bayesian) predict_inlier_body(c.d); });
+}
 
 // Candidates owning at least one vertex (and so a mesh page), for the
 // inlier prediction; one thread per candidate, warp-ballot compaction.
-__global__ void __launch_bounds__(256) k_vtx_select(Dev d) {
+__device__ __forceinline__ void vtx_select_body(const Dev &d) {
   const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -310,10 +323,14 @@ __global__ void __launch_bounds__(256) k_vtx_select(Dev d) {
     if (keep) d.vtx_list[slot + __popc(m & lanemask_lt())] = i;
   }
 }
+__global__ void __launch_bounds__(256) k_vtx_select(Dev d) { vtx_select_body(d); }
+__global__ void __launch_bounds__(256) k_vtx_select_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { if (c.d.p.enable_bayesian) vtx_select_body(c.d); });
+}
 
 // Sensor::Process tail: depth validity (ConvertDepthFormatKernel,
 // sensor/preprocess.cu:25-42) and inlier-ratio reset to 0.1 (:10-23).
-__global__ void k_preprocess(Dev d, const float *src, const uint16_t *src16, float range_factor) {
+__device__ __forceinline__ void preprocess_body(const Dev &d, const float *src, const uint16_t *src16, float range_factor) {
   const int n = d.p.width * d.p.height;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float z = src16 ? range_factor * (float)src16[i] : src[i];
@@ -321,6 +338,10 @@ __global__ void k_preprocess(Dev d, const float *src, const uint16_t *src16, flo
     d.depth[i] = ok ? z : -__int_as_float(0x7f800000);
     d.inlier[i] = 0.1f;
   }
+}
+__global__ void k_preprocess(Dev d, const float *src, const uint16_t *src16, float range_factor) { preprocess_body(d, src, src16, range_factor); }
+__global__ void k_preprocess_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { preprocess_body(c.d, c.src, nullptr, 0.0f); });
 }
 
 static int grid_persistent(int per_sm) { return mh_sm_count() * per_sm; }
@@ -346,4 +367,36 @@ int launch_preprocess(const Dev &d, const float *src, const uint16_t *src16, flo
   k_preprocess<<<grid_persistent(4), 256, 0, s>>>(d, src, src16, range_factor);
   mh_count_launches(1);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+
+// ------------------------------------------------------------------ batched
+int launch_batch_preprocess(const Scene *t, int n, cudaStream_t s) {
+  k_preprocess_b<<<mh_sm_count() * 4, 256, 0, s>>>(t, n);
+  mh_count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+int launch_batch_predict(const Scene *t, int n, cudaStream_t s) {
+  k_vtx_select_b<<<mh_sm_count() * 4, 256, 0, s>>>(t, n);
+  k_predict_inlier_b<<<mh_resident_grid((const void *)k_predict_inlier_b, 128, 16), 128, 0, s>>>(t, n);
+  mh_count_launches(2);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+// cta_per_sm caps the persistent grid (an autotuned choice)
+int launch_batch_integrate(const Scene *t, int n, int has_simple, int has_psdf, int cta_per_sm, cudaStream_t s) {
+  if (has_simple) {
+    k_integrate_simple_b<<<mh_resident_grid((const void *)k_integrate_simple_b, 128, cta_per_sm), 128, 0, s>>>(t, n);
+    mh_count_launches(1);
+  }
+  if (has_psdf) {
+    k_integrate_psdf_b<<<mh_resident_grid((const void *)k_integrate_psdf_b, 128, cta_per_sm), 128, 0, s>>>(t, n);
+    mh_count_launches(1);
+  }
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+// the occupancy queries of the batched persistent grids, made before any
+// stream capture
+void batch_warm_occupancy() {
+  mh_resident_grid((const void *)k_predict_inlier_b, 128, 16);
+  mh_resident_grid((const void *)k_integrate_simple_b, 128, 16);
+  mh_resident_grid((const void *)k_integrate_psdf_b, 128, 16);
 }

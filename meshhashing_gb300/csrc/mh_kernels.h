@@ -4,6 +4,8 @@
 
 #include "mh_internal.cuh"
 
+struct Scene;
+
 int launch_alloc(const Dev &d, cudaStream_t s);
 int launch_collect(const Dev &d, int frustum, cudaStream_t s);
 int launch_insert_list(const Dev &d, const int *pos_dev, int n, cudaStream_t s);
@@ -25,3 +27,19 @@ int launch_gc_collect_garbage(const Dev &d, cudaStream_t s);
 int launch_gc_recycle(const Dev &d, cudaStream_t s);
 
 int launch_denoise_tv(const Dev &d, float *tv, float lambda, int iterations, cudaStream_t s);
+
+// batched twins: one launch per stage for every active scene of a scene table
+int launch_batch_preprocess(const Scene *t, int n, cudaStream_t s);
+int launch_batch_tv(const Scene *t, int n, int max_pixels, float lambda, int iterations, cudaStream_t s);
+int launch_batch_alloc(const Scene *t, int n, int total_tiles, cudaStream_t s);
+int launch_batch_collect(const Scene *t, int n, cudaStream_t s);
+int launch_batch_predict(const Scene *t, int n, cudaStream_t s);
+int launch_batch_integrate(const Scene *t, int n, int has_simple, int has_psdf, int cta_per_sm, cudaStream_t s);
+int launch_batch_mesh(const Scene *t, int n, cudaStream_t s);
+int launch_batch_gc_low_surfel(const Scene *t, int n, cudaStream_t s);
+int launch_batch_gc_recycle(const Scene *t, int n, int which, cudaStream_t s);
+int launch_batch_gc_starve(const Scene *t, int n, cudaStream_t s);
+int launch_raycast_batch(const Scene *t, int n, int total_tiles, int shape, cudaStream_t s);
+int ray_tile_shapes();
+void ray_tile_shape(int i, int &tx, int &ty);
+void batch_warm_occupancy();

@@ -34,6 +34,7 @@
 // passes walk only the candidates that hold a page.
 #include "mh_internal.cuh"
 #include "mh_kernels.h"
+#include "mh_batch.cuh"
 
 #define MH_MC_TABLE_QUALIFIER __constant__
 #include "mc_cases.inc"
@@ -69,17 +70,21 @@ __device__ __forceinline__ bool claim_slot(const Dev &d, uint32_t *cw, int slot,
   return false;
 }
 
-__global__ void k_mc_begin(Dev d) {
+__device__ __forceinline__ void mc_begin_body(const Dev &d) {
   d.ctr->epoch += 1;
   d.ctr->vwork_count = 0;
   d.ctr->mesh_list_count = 0;
   d.ctr->cube_list_count = 0;
 }
+__global__ void k_mc_begin(Dev d) { mc_begin_body(d); }
+__global__ void k_mc_begin_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { mc_begin_body(c.d); });
+}
 
 // Candidates the cube pass must tile: a block holding a mesh page, or one
 // whose weight bound reaches the MC gate (otherwise no cube in it is valid).
 // One thread per candidate, warp-ballot compaction.
-__global__ void __launch_bounds__(256) k_mc_select(Dev d) {
+__device__ __forceinline__ void mc_select_body(const Dev &d) {
   const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
   const float lim = 1.0f / d.p.voxel_size;
   const float lim2 = lim * lim;
@@ -99,15 +104,23 @@ __global__ void __launch_bounds__(256) k_mc_select(Dev d) {
     if (keep) d.cube_list[slot + __popc(m & lanemask_lt())] = cb;
   }
 }
-__global__ void k_mc_end(Dev d) {
+__global__ void __launch_bounds__(256) k_mc_select(Dev d) { mc_select_body(d); }
+__global__ void __launch_bounds__(256) k_mc_select_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { mc_select_body(c.d); });
+}
+__device__ __forceinline__ void mc_end_body(const Dev &d) {
   d.ctr->mesh_passes += 1;
   d.ctr->cand_sum += (unsigned long long)d.ctr->cand_count;
   d.ctr->vwork_sum += (unsigned long long)min(d.ctr->vwork_count, d.vwork_capacity);
   d.ctr->mesh_list_sum += (unsigned long long)d.ctr->mesh_list_count;
 }
+__global__ void k_mc_end(Dev d) { mc_end_body(d); }
+__global__ void k_mc_end_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { mc_end_body(c.d); });
+}
 
 // ------------------------------------------------------------------ pass 1
-__global__ void __launch_bounds__(512) k_mc_cubes(Dev d) {
+__device__ __forceinline__ void mc_cubes_body(const Dev &d) {
   __shared__ uint8_t tile[729];
   __shared__ int nb[8];
   __shared__ int own_page;
@@ -175,9 +188,13 @@ __global__ void __launch_bounds__(512) k_mc_cubes(Dev d) {
     __syncthreads();
   }
 }
+__global__ void __launch_bounds__(512) k_mc_cubes(Dev d) { mc_cubes_body(d); }
+__global__ void __launch_bounds__(512) k_mc_cubes_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { mc_cubes_body(c.d); });
+}
 
 // candidates holding a page after pass 1; the others get zero surfel counts
-__global__ void __launch_bounds__(256) k_mc_list(Dev d) {
+__device__ __forceinline__ void mc_list_body(const Dev &d) {
   const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
   const int stride = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -198,9 +215,13 @@ __global__ void __launch_bounds__(256) k_mc_list(Dev d) {
     if (keep) d.mesh_list[slot + __popc(m & lanemask_lt())] = ptr;
   }
 }
+__global__ void __launch_bounds__(256) k_mc_list(Dev d) { mc_list_body(d); }
+__global__ void __launch_bounds__(256) k_mc_list_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { mc_list_body(c.d); });
+}
 
 // ------------------------------------------------------------------ vertices
-__global__ void __launch_bounds__(128) k_mc_vertices(Dev d) {
+__device__ __forceinline__ void mc_vertices_body(const Dev &d) {
   const int n = min(*reinterpret_cast<volatile int *>(&d.ctr->vwork_count), d.vwork_capacity);
   const int stride = gridDim.x * blockDim.x;
   const float vs = d.p.voxel_size;
@@ -273,9 +294,13 @@ __global__ void __launch_bounds__(128) k_mc_vertices(Dev d) {
     v4[1] = make_float4(nrm.y, nrm.z, radius, __int_as_float(ref));
   }
 }
+__global__ void __launch_bounds__(128) k_mc_vertices(Dev d) { mc_vertices_body(d); }
+__global__ void __launch_bounds__(128) k_mc_vertices_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { mc_vertices_body(c.d); });
+}
 
 // ------------------------------------------------------------------ pass 2
-__global__ void __launch_bounds__(512) k_mc_triangles(Dev d) {
+__device__ __forceinline__ void mc_triangles_body(const Dev &d) {
   __shared__ int nbp[8];
   __shared__ int cnt[2];
   const int tid = threadIdx.x;
@@ -354,9 +379,13 @@ __global__ void __launch_bounds__(512) k_mc_triangles(Dev d) {
     __syncthreads();
   }
 }
+__global__ void __launch_bounds__(512) k_mc_triangles(Dev d) { mc_triangles_body(d); }
+__global__ void __launch_bounds__(512) k_mc_triangles_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { mc_triangles_body(c.d); });
+}
 
 // ------------------------------------------------------------------ recycle
-__global__ void __launch_bounds__(128) k_mc_recycle_tri(Dev d) {
+__device__ __forceinline__ void mc_recycle_tri_body(const Dev &d) {
   const int n = *reinterpret_cast<volatile int *>(&d.ctr->mesh_list_count);
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
     const int pg = d.page_of[d.mesh_list[c]];
@@ -379,8 +408,12 @@ __global__ void __launch_bounds__(128) k_mc_recycle_tri(Dev d) {
     }
   }
 }
+__global__ void __launch_bounds__(128) k_mc_recycle_tri(Dev d) { mc_recycle_tri_body(d); }
+__global__ void __launch_bounds__(128) k_mc_recycle_tri_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { mc_recycle_tri_body(c.d); });
+}
 
-__global__ void __launch_bounds__(128) k_mc_recycle_vtx(Dev d) {
+__device__ __forceinline__ void mc_recycle_vtx_body(const Dev &d) {
   __shared__ int live;
   const int n = *reinterpret_cast<volatile int *>(&d.ctr->mesh_list_count);
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
@@ -415,6 +448,10 @@ __global__ void __launch_bounds__(128) k_mc_recycle_vtx(Dev d) {
     __syncthreads();
   }
 }
+__global__ void __launch_bounds__(128) k_mc_recycle_vtx(Dev d) { mc_recycle_vtx_body(d); }
+__global__ void __launch_bounds__(128) k_mc_recycle_vtx_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) { mc_recycle_vtx_body(c.d); });
+}
 
 int launch_mesh(const Dev &d, cudaStream_t s) {
   const int sms = mh_sm_count();
@@ -427,6 +464,21 @@ int launch_mesh(const Dev &d, cudaStream_t s) {
   k_mc_recycle_tri<<<sms * 8, 128, 0, s>>>(d);
   k_mc_recycle_vtx<<<sms * 8, 128, 0, s>>>(d);
   k_mc_end<<<1, 1, 0, s>>>(d);
+  mh_count_launches(9);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+
+int launch_batch_mesh(const Scene *t, int n, cudaStream_t s) {
+  const int sms = mh_sm_count();
+  k_mc_begin_b<<<1, 1, 0, s>>>(t, n);
+  k_mc_select_b<<<sms * 4, 256, 0, s>>>(t, n);
+  k_mc_cubes_b<<<sms * 2, 512, 0, s>>>(t, n);
+  k_mc_list_b<<<sms * 4, 256, 0, s>>>(t, n);
+  k_mc_vertices_b<<<sms * 8, 128, 0, s>>>(t, n);
+  k_mc_triangles_b<<<sms * 2, 512, 0, s>>>(t, n);
+  k_mc_recycle_tri_b<<<sms * 8, 128, 0, s>>>(t, n);
+  k_mc_recycle_vtx_b<<<sms * 8, 128, 0, s>>>(t, n);
+  k_mc_end_b<<<1, 1, 0, s>>>(t, n);
   mh_count_launches(9);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }

@@ -30,6 +30,9 @@
 //    blocks at about the same t.
 #include "mh_internal.cuh"
 #include "mh_kernels.h"
+#include "mh_batch.cuh"
+
+#include <algorithm>
 
 #define RC_TX 16
 #define RC_TY 8
@@ -164,16 +167,17 @@ __device__ __forceinline__ bool ray_gradient(const Dev &d, RayCache &c, F3 pos, 
 
 }  // namespace
 
-__global__ void __launch_bounds__(RC_TX *RC_TY) k_raycast(Dev d, float *out_depth, float4 *out_vert, float4 *out_norm) {
+template <int TX, int TY>
+__device__ __forceinline__ void raycast_body(const Dev &d, int tile_x, int tile_y, float *out_depth, float4 *out_vert, float4 *out_norm) {
   __shared__ float sm[32];
-  const int tid = threadIdx.x + threadIdx.y * RC_TX;
+  const int tid = threadIdx.x + threadIdx.y * TX;
   if (tid < 16) sm[tid] = d.fc->rc_wTc[tid];
   else if (tid < 32) sm[tid] = d.fc->rc_cTw[tid - 16];
   __syncthreads();
   const float *wTc = sm, *cTw = sm + 16;
   const DevParams &p = d.p;
-  const unsigned x = blockIdx.x * RC_TX + threadIdx.x;
-  const unsigned y = blockIdx.y * RC_TY + threadIdx.y;
+  const unsigned x = tile_x * TX + threadIdx.x;
+  const unsigned y = tile_y * TY + threadIdx.y;
   if (x >= p.rc_width || y >= p.rc_height) return;
   const size_t pix = (size_t)y * p.rc_width + x;
   const float NI = -__int_as_float(0x7f800000);
@@ -248,6 +252,35 @@ __global__ void __launch_bounds__(RC_TX *RC_TY) k_raycast(Dev d, float *out_dept
   if (out_depth) out_depth[pix] = o_depth;
   if (out_vert) out_vert[pix] = o_vert;
   if (out_norm) out_norm[pix] = o_norm;
+}
+__global__ void __launch_bounds__(RC_TX *RC_TY) k_raycast(Dev d, float *out_depth, float4 *out_vert, float4 *out_norm) { raycast_body<RC_TX, RC_TY>(d, blockIdx.x, blockIdx.y, out_depth, out_vert, out_norm); }
+// batched raycast over the scenes' concatenated TX x TY tiles; the tile shape
+// is an autotuned choice (the scene table's ray_tile0 follows it)
+template <int TX, int TY>
+__global__ void __launch_bounds__(TX *TY, 65536 / (TX * TY * 72)) k_raycast_b(const Scene *t, int n, int total) {
+  each_tile(t, n, total, &Scene::ray_tile0, [&](const Scene &c, int lt) {
+    const int tw = (c.d.p.rc_width + TX - 1) / TX;
+    raycast_body<TX, TY>(c.d, lt % tw, lt / tw, c.ray_depth, c.ray_vert, c.ray_norm);
+  });
+}
+
+// tile shapes the batch autotuner chooses from
+static const int kRayTiles[][2] = {{16, 8}, {8, 8}, {32, 4}};
+int ray_tile_shapes() { return 3; }
+void ray_tile_shape(int i, int &tx, int &ty) {
+  tx = kRayTiles[i][0];
+  ty = kRayTiles[i][1];
+}
+
+int launch_raycast_batch(const Scene *t, int n, int total, int shape, cudaStream_t s) {
+  const int grid = std::max(1, std::min(total, mh_sm_count() * 16));
+  switch (shape) {
+    case 1: k_raycast_b<8, 8><<<grid, dim3(8, 8), 0, s>>>(t, n, total); break;
+    case 2: k_raycast_b<32, 4><<<grid, dim3(32, 4), 0, s>>>(t, n, total); break;
+    default: k_raycast_b<16, 8><<<grid, dim3(16, 8), 0, s>>>(t, n, total); break;
+  }
+  mh_count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }
 
 int launch_raycast(const Dev &d, float *depth, float *vert4, float *norm4, cudaStream_t s) {

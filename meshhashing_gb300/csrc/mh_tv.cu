@@ -17,6 +17,9 @@
 // tiling.
 #include "mh_internal.cuh"
 #include "mh_kernels.h"
+#include "mh_batch.cuh"
+
+#include <algorithm>
 
 namespace {
 
@@ -46,7 +49,7 @@ __device__ __forceinline__ void dual_at(const TvBuf &b, int x, int y, float sigm
 
 }  // namespace
 
-__global__ void k_tv_init(const float *depth, float *f, float *u, float *ub, float *px, float *py, int n) {
+__device__ __forceinline__ void tv_init_body(const float *depth, float *f, float *u, float *ub, float *px, float *py, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float z = depth[i];
     const bool ok = z > 0.0f && z < 1e30f;
@@ -58,8 +61,15 @@ __global__ void k_tv_init(const float *depth, float *f, float *u, float *ub, flo
     py[i] = 0.0f;
   }
 }
+__global__ void k_tv_init(const float *depth, float *f, float *u, float *ub, float *px, float *py, int n) { tv_init_body(depth, f, u, ub, px, py, n); }
+__global__ void k_tv_init_b(const Scene *t, int n) {
+  each_scene(t, n, [&](const Scene &c) {
+    const size_t np = (size_t)c.d.p.width * c.d.p.height;
+    tv_init_body(c.d.depth, c.tv, c.tv + np, c.tv + 2 * np, c.tv + 3 * np, c.tv + 4 * np, (int)np);
+  });
+}
 
-__global__ void __launch_bounds__(256) k_tv_iter(TvBuf b) {
+__device__ __forceinline__ void tv_iter_body(const TvBuf &b) {
   const float tau = 0.35355339059327373f, sigma = 0.35355339059327373f;
   const int n = b.W * b.H;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -83,10 +93,32 @@ __global__ void __launch_bounds__(256) k_tv_iter(TvBuf b) {
     b.ub2[i] = 2.0f * un - u0;
   }
 }
+__global__ void __launch_bounds__(256) k_tv_iter(TvBuf b) { tv_iter_body(b); }
+// iteration `it` of a batch: planes 1-4 hold the iterate after an even number
+// of iterations, planes 5-8 after an odd number
+__global__ void __launch_bounds__(256) k_tv_iter_b(const Scene *t, int n, int it, float lambda) {
+  each_scene(t, n, [&](const Scene &c) {
+    const size_t np = (size_t)c.d.p.width * c.d.p.height;
+    float *A = c.tv + np * ((it & 1) ? 5 : 1), *B = c.tv + np * ((it & 1) ? 1 : 5);
+    TvBuf b;
+    b.f = c.tv;
+    b.u = A, b.ub = A + np, b.px = A + 2 * np, b.py = A + 3 * np;
+    b.u2 = B, b.ub2 = B + np, b.px2 = B + 2 * np, b.py2 = B + 3 * np;
+    b.W = c.d.p.width, b.H = c.d.p.height, b.lambda = lambda;
+    tv_iter_body(b);
+  });
+}
 
-__global__ void k_tv_out(const float *f, const float *u, float *depth, int n) {
+__device__ __forceinline__ void tv_out_body(const float *f, const float *u, float *depth, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     depth[i] = valid_at(f, i) ? u[i] * 0.001f : -__int_as_float(0x7f800000);
+}
+__global__ void k_tv_out(const float *f, const float *u, float *depth, int n) { tv_out_body(f, u, depth, n); }
+__global__ void k_tv_out_b(const Scene *t, int n, int iterations) {
+  each_scene(t, n, [&](const Scene &c) {
+    const size_t np = (size_t)c.d.p.width * c.d.p.height;
+    tv_out_body(c.tv, c.tv + np * ((iterations & 1) ? 5 : 1), c.d.depth, (int)np);
+  });
 }
 
 // tv holds 9 planes of W*H floats: f, (u, ub, px, py) x 2
@@ -171,6 +203,16 @@ extern "C" int mh_denoise_tv_static(const float *depth_in, float *depth_out, int
     }
   }
   k_tv_out<<<g, 256, 0, s>>>(f, A[0], depth_out, n);
+  mh_count_launches(2 + iterations);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+
+// ------------------------------------------------------------------ batched
+int launch_batch_tv(const Scene *t, int n, int max_pixels, float lambda, int iterations, cudaStream_t s) {
+  const int g = std::max(1, std::min((max_pixels + 255) / 256, mh_sm_count() * 8));
+  k_tv_init_b<<<g, 256, 0, s>>>(t, n);
+  for (int it = 0; it < iterations; ++it) k_tv_iter_b<<<g, 256, 0, s>>>(t, n, it, lambda);
+  k_tv_out_b<<<g, 256, 0, s>>>(t, n, iterations);
   mh_count_launches(2 + iterations);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }

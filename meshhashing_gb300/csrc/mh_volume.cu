@@ -18,33 +18,8 @@
 
 #include "mh_internal.cuh"
 #include "mh_kernels.h"
+#include "mh_volume.h"
 
-struct mh_volume {
-  mh_params hp;
-  Dev d;
-  float *tv = nullptr;
-  float *rc_stage = nullptr;  // device staging for host raycast outputs
-  int *scratch = nullptr;     // device scratch for list operations
-  size_t scratch_bytes = 0;
-  FrameConst fc_host;
-  bool has_frame = false;
-  int frames = 0;
-  std::vector<void *> allocs;
-  // per-stage CUDA-event timing (events are pooled and reused)
-  bool prof = false;
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pend[MH_STAGE_COUNT];
-  std::vector<cudaEvent_t> ev_pool;
-  cudaEvent_t event() {
-    cudaEvent_t e = nullptr;
-    if (!ev_pool.empty()) {
-      e = ev_pool.back();
-      ev_pool.pop_back();
-    } else {
-      cudaEventCreate(&e);
-    }
-    return e;
-  }
-};
 
 static std::atomic<unsigned long long> g_launches{0};
 void mh_count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
@@ -102,7 +77,7 @@ int mh_resident_grid(const void *fn, int block, int cap_per_sm) {
 
 // 4x4 inverse by cofactors with the term order of float4x4::getInverse
 // (extern/cuda/matrix.h:964-1086); compiled without FMA contraction.
-static void inverse4(const float *m, float *out) {
+void inverse4(const float *m, float *out) {
   float inv[16];
   for (int r = 0; r < 4; ++r) {
     for (int c = 0; c < 4; ++c) {
