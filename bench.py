@@ -146,6 +146,127 @@ def bytes_per_launch(stage, nb, px, rpx, vwork, cube_blocks=0, mesh_blocks=0, pr
     return 0.0
 
 
+# ---------------------------------------------------------------- batched scenes
+BATCH_RES = ((160, 120), (320, 240), (640, 480))
+BATCH_VOXEL = (0.004, 0.006, 0.008)
+
+
+def batch_specs(n_scenes):
+    """Scene s: room generator seed s, frame count U[20, 200], resolution and
+    voxel size drawn from the batched-fusion workload's sets (seeded)."""
+    rng = np.random.default_rng(12345)
+    out = []
+    for s in range(n_scenes):
+        w, h = BATCH_RES[rng.integers(0, 3)]
+        out.append(dict(seed=s, frames=int(rng.integers(20, 201)), width=w, height=h,
+                        voxel=float(BATCH_VOXEL[rng.integers(0, 3)])))
+    return out
+
+
+def _batch_frame_job(args):
+    spec, i = args
+    from meshhashing_gb300 import scene
+    wl = scene.full_spline(spec["frames"], seed=spec["seed"], width=spec["width"], height=spec["height"])
+    return wl.frame(i), wl.pose(i)
+
+
+def gen_batch_frames(specs, n):
+    ctx = mp.get_context("spawn")
+    jobs = [(sp, i) for sp in specs for i in range(n)]
+    with ctx.Pool(min(os.cpu_count() or 4, 16)) as pool:
+        out = pool.map(_batch_frame_job, jobs, chunksize=4)
+    frames = [[out[k * n + i][0] for i in range(n)] for k in range(len(specs))]
+    poses = [[out[k * n + i][1] for i in range(n)] for k in range(len(specs))]
+    return frames, poses
+
+
+def batch_params(spec):
+    from meshhashing_gb300 import config, scene
+    wl = scene.full_spline(spec["frames"], seed=spec["seed"], width=spec["width"], height=spec["height"])
+    px = spec["width"] * spec["height"]
+    log2 = {19200: 15, 76800: 17, 307200: 19}[px] - (1 if px == 307200 and spec["voxel"] > 0.004 else 0)
+    return config.params_for(wl, voxel_size=spec["voxel"], truncation=3 * spec["voxel"], value_capacity=1 << log2,
+                             bucket_count=1 << max(log2, 14), max_vertex_count=1 << (log2 + 1),
+                             max_triangle_count=1 << (log2 + 1), overflow_capacity=1 << max(log2 - 2, 10),
+                             mesh_page_capacity=1 << (log2 - 3))
+
+
+def run_batched(specs, frames, poses, P, W, K):
+    """Aggregate frames/s of the scenes advanced one after another with the
+    plain per-frame chain, then (same volumes, reset) as one batch: one launch
+    per stage for all scenes, autotuned during the P pre-fuse steps, the step
+    replayed from a CUDA graph."""
+    import torch
+    from meshhashing_gb300 import Batch, Volume
+    n = len(specs)
+    vols = [Volume(batch_params(sp)) for sp in specs]
+    dev = [torch.from_numpy(np.stack(f)).cuda() for f in frames]
+    outs = [torch.empty((sp["height"], sp["width"]), dtype=torch.float32, device="cuda") for sp in specs]
+
+    def plain(i):
+        for s in range(n):
+            vols[s].integrate_frame(dev[s][i], poses[s][i], on_device=True, tv_iterations=TV_ITERS,
+                                    tv_lambda=TV_LAMBDA, ray_depth=outs[s], outputs_on_device=True)
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for i in range(P + W):
+        plain(i)
+    torch.cuda.synchronize()
+    e0.record()
+    for i in range(P + W, P + W + K):
+        plain(i)
+    e1.record()
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    err_plain = sum(v.stats()["error"] != 0 for v in vols)
+    for v in vols:
+        v.reset()
+    batch = Batch(vols, raycast=True)
+    batch.autotune(max(1, P // 9))
+
+    def bstep(i, graph):
+        batch.step([dev[s][i] for s in range(n)], [poses[s][i] for s in range(n)], on_device=True,
+                   tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA, use_graph=graph)
+
+    for i in range(P):
+        bstep(i, False)
+    for i in range(P, P + W):
+        bstep(i, True)
+    torch.cuda.synchronize()
+    e0.record()
+    for i in range(P + W, P + W + K):
+        bstep(i, True)
+    e1.record()
+    torch.cuda.synchronize()
+    batch_ms = e0.elapsed_time(e1)
+    err_batch = sum(v.stats()["error"] != 0 for v in vols)
+    tuning, times = batch.tuning(), batch.tuning_times()
+    batch.close()
+    for v in vols:
+        v.close()
+    res = {}
+    for sp in specs:
+        k = "%dx%d" % (sp["width"], sp["height"])
+        res[k] = res.get(k, 0) + 1
+    vox = {}
+    for sp in specs:
+        k = "%d" % round(sp["voxel"] * 1000)
+        vox[k] = vox.get(k, 0) + 1
+    frames_per_step = n
+    return {"workload": "%d independent room scenes (seeds 0..%d), PSDF, TV %d it, raycast" % (n, n - 1, TV_ITERS),
+            "scenes": n, "resolutions": res, "voxel_mm": vox, "steps": K, "warmup": W, "prefuse": P,
+            "value": frames_per_step * K / (batch_ms / 1000.0), "unit": "frames/s (all scenes)",
+            "plain_value": frames_per_step * K / (plain_ms / 1000.0),
+            "speedup_vs_plain": plain_ms / batch_ms, "ms_per_step": batch_ms / K, "plain_ms_per_step": plain_ms / K,
+            "form": "one launch per stage for all scenes, step replayed from a CUDA graph",
+            "plain_form": "scenes one after another, per-frame stream launches",
+            "tuning": {"chosen": {"ray_tile": list(tuning["ray_tile"]),
+                                  "integrate_cta_per_sm": tuning["integrate_cta_per_sm"]},
+                       "raycast_ms": {"%dx%d" % k: v for k, v in times["raycast_ms"].items()},
+                       "integrate_ms": {str(k): v for k, v in times["integrate_ms"].items()}},
+            "scenes_with_error": {"plain": int(err_plain), "batched": int(err_batch)}}
+
+
 def run_cpu_baseline(params, frames, poses, threads=None):
     """FP64 oracle on all host threads, from an empty volume."""
     from oracle import oracle as O
@@ -200,6 +321,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-frames", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-scenes", type=int, default=64,
+                    help="scenes of the batched-vs-plain measurement (0: skip it)")
+    ap.add_argument("--batch-steps", type=int, default=5)
     ap.add_argument("--capacity-log2", type=int, default=21,
                     help="block pool size (2^n blocks); smaller values for profiler captures")
     args = ap.parse_args()
@@ -219,6 +343,10 @@ def main():
     cpu_frames = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu_frames = (frames[:args.cpu_frames], poses[:args.cpu_frames])
+
+    bspecs = batch_specs(args.batch_scenes) if (args.batch_scenes > 0 and world == 1) else []
+    BP, BW, BK = 9, 3, args.batch_steps
+    bframes = gen_batch_frames(bspecs, BP + BW + BK) if bspecs else None
 
     import torch
     torch.cuda.set_device(local)
@@ -318,6 +446,9 @@ def main():
             gbs = b / ((t_ms / c) / 1000.0) / 1e9 if t_ms > 0 else None
             stages[k] = {"ms_per_frame": t_ms / K, "gbs": gbs, "frac": (gbs / peak) if gbs else None}
 
+    vol.close()
+    batched = run_batched(bspecs, bframes[0], bframes[1], BP, BW, BK) if bspecs else None
+
     cpu = None
     if cpu_frames is not None:
         fps, cores, dt = run_cpu_baseline(params, *cpu_frames)
@@ -344,9 +475,9 @@ def main():
                           "allocated": s2["blocks_allocated"], "mesh_pages": s2["mesh_pages_used"],
                           "error": s2["error"]},
                "clocks": clocks,
+               "batched": batched,
                "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
-    vol.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 

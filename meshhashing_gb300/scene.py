@@ -174,7 +174,8 @@ def room_scene(seed: int, extra: int = 0) -> Scene:
         size = rng.uniform(0.08, 0.25)
         while True:
             ang = rng.uniform(0, 2 * math.pi)
-            rad = rng.choice([rng.uniform(0.0, 0.7 - size), rng.uniform(1.55 + size, 2.0 - size)])
+            # (the outer ring is empty for size > 0.225: its range collapses to a point)
+            rad = rng.choice([rng.uniform(0.0, 0.7 - size), rng.uniform(1.55 + size, max(2.0 - size, 1.55 + size))])
             x, y = rad * math.cos(ang), rad * math.sin(ang)
             if abs(x) <= 2.0 - size and abs(y) <= 2.0 - size:
                 break
