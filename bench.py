@@ -180,15 +180,18 @@ def gen_batch_frames(specs, n):
     return frames, poses
 
 
-def batch_params(spec):
+def batch_params(spec, frames_run):
+    """Pools sized for frames_run frames of the outlier-heavy stream: ~7.5 % of
+    the pixels allocate a block per frame (5 % outliers) plus the surface."""
     from meshhashing_gb300 import config, scene
     wl = scene.full_spline(spec["frames"], seed=spec["seed"], width=spec["width"], height=spec["height"])
     px = spec["width"] * spec["height"]
-    log2 = {19200: 15, 76800: 17, 307200: 19}[px] - (1 if px == 307200 and spec["voxel"] > 0.004 else 0)
-    return config.params_for(wl, voxel_size=spec["voxel"], truncation=3 * spec["voxel"], value_capacity=1 << log2,
-                             bucket_count=1 << max(log2, 14), max_vertex_count=1 << (log2 + 1),
-                             max_triangle_count=1 << (log2 + 1), overflow_capacity=1 << max(log2 - 2, 10),
-                             mesh_page_capacity=1 << (log2 - 3))
+    cap = int(px * (0.075 * frames_run + 0.6) * 1.4) // 1024 * 1024 + 1024
+    buckets = 1 << max(14, (cap - 1).bit_length())
+    pools = 1 << max(15, (cap // 2 - 1).bit_length())
+    return config.params_for(wl, voxel_size=spec["voxel"], truncation=3 * spec["voxel"], value_capacity=cap,
+                             bucket_count=buckets, max_vertex_count=pools, max_triangle_count=pools,
+                             overflow_capacity=max(buckets // 4, 1024), mesh_page_capacity=max(cap // 64, 2048))
 
 
 def run_batched(specs, frames, poses, P, W, K):
@@ -199,7 +202,7 @@ def run_batched(specs, frames, poses, P, W, K):
     import torch
     from meshhashing_gb300 import Batch, Volume
     n = len(specs)
-    vols = [Volume(batch_params(sp)) for sp in specs]
+    vols = [Volume(batch_params(sp, P + W + K)) for sp in specs]
     dev = [torch.from_numpy(np.stack(f)).cuda() for f in frames]
     outs = [torch.empty((sp["height"], sp["width"]), dtype=torch.float32, device="cuda") for sp in specs]
 
@@ -240,7 +243,7 @@ def run_batched(specs, frames, poses, P, W, K):
     torch.cuda.synchronize()
     batch_ms = e0.elapsed_time(e1)
     err_batch = sum(v.stats()["error"] != 0 for v in vols)
-    tuning, times = batch.tuning(), batch.tuning_times()
+    tuning, times, stage = batch.tuning(), batch.tuning_times(), batch.stage_times()
     batch.close()
     for v in vols:
         v.close()
@@ -264,6 +267,7 @@ def run_batched(specs, frames, poses, P, W, K):
                                   "integrate_cta_per_sm": tuning["integrate_cta_per_sm"]},
                        "raycast_ms": {"%dx%d" % k: v for k, v in times["raycast_ms"].items()},
                        "integrate_ms": {str(k): v for k, v in times["integrate_ms"].items()}},
+            "stage_ms_per_step": stage,
             "scenes_with_error": {"plain": int(err_plain), "batched": int(err_batch)}}
 
 
@@ -447,7 +451,12 @@ def main():
             stages[k] = {"ms_per_frame": t_ms / K, "gbs": gbs, "frac": (gbs / peak) if gbs else None}
 
     vol.close()
-    batched = run_batched(bspecs, bframes[0], bframes[1], BP, BW, BK) if bspecs else None
+    batched = None
+    if bspecs:
+        batched = run_batched(bspecs, bframes[0], bframes[1], BP, BW, BK)
+        small = [k for k, sp in enumerate(bspecs) if sp["width"] < 640]
+        batched["below_640x480"] = run_batched([bspecs[k] for k in small], [bframes[0][k] for k in small],
+                                               [bframes[1][k] for k in small], BP, BW, BK)
 
     cpu = None
     if cpu_frames is not None:

@@ -301,6 +301,9 @@ int mh_batch_autotune(mh_batch *b, int trials);
 /* ms per step of the integrate and raycast stages measured by the autotuner
  * for each choice (3 shapes, 3 caps), -1 where not measured */
 int mh_batch_tuning_times(mh_batch *b, double ray_ms[3], double integrate_ms[3]);
+/* ms per step of each stage (MH_STAGE_*) averaged over the autotuning steps,
+ * -1 before any; the raycast entry covers the raycast only */
+int mh_batch_stage_times(mh_batch *b, double ms[MH_STAGE_COUNT]);
 
 uint32_t mh_hash_bucket(int32_t x, int32_t y, int32_t z, uint32_t bucket_count);
 /* Bytes the last frame's stages needed by the algorithmic model (see the

@@ -70,6 +70,7 @@ SIGNATURES = {
     "mh_batch_set_tuning": (i32, [vp, C.POINTER(MhBatchTuning)]),
     "mh_batch_autotune": (i32, [vp, i32]),
     "mh_batch_tuning_times": (i32, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "mh_batch_stage_times": (i32, [vp, C.POINTER(C.c_double)]),
 }
 SYMBOLS = sorted(SIGNATURES)
 

@@ -107,3 +107,11 @@ class Batch:
         self._c("mh_batch_tuning_times", r, i)
         return {"raycast_ms": dict(zip(RAY_TILE_SHAPES, list(r))),
                 "integrate_ms": dict(zip(INTEGRATE_CTA_CAPS, list(i)))}
+
+    STAGES = ("preprocess", "tv", "alloc", "collect", "predict", "integrate", "mesh", "gc", "raycast")
+
+    def stage_times(self):
+        """ms per step of each stage, averaged over the autotuning steps."""
+        ms = (C.c_double * 9)()
+        self._c("mh_batch_stage_times", ms)
+        return dict(zip(self.STAGES, list(ms)))

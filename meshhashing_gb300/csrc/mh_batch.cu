@@ -64,6 +64,10 @@ struct mh_batch {
   double ray_ms[3] = {0, 0, 0}, int_ms[3] = {0, 0, 0};
   int ray_cnt[3] = {0, 0, 0}, int_cnt[3] = {0, 0, 0};
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // per-stage times of the tuning steps (events at every stage boundary)
+  cudaEvent_t sev[MH_STAGE_COUNT + 1] = {};
+  double stage_ms[MH_STAGE_COUNT] = {};
+  int stage_steps = 0;
 
   Scene *table() const { return reinterpret_cast<Scene *>(d_block); }
   int ray_tiles(int shape, std::vector<int> *first) const {
@@ -87,6 +91,8 @@ static void batch_free(mh_batch *b) {
   }
   for (cudaEvent_t e : b->ev)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : b->sev)
+    if (e) cudaEventDestroy(e);
   for (void *p : b->allocs) cudaFree(p);
   if (b->own) cudaStreamDestroy(b->own);
   delete b;
@@ -102,20 +108,32 @@ static int enqueue(mh_batch *b, int p, bool host_depth, int tv_it, float lambda,
     MH_CUDA_TRY(cudaMemcpyAsync(b->d_depth, b->h_depth[p], b->pixels * sizeof(float), cudaMemcpyHostToDevice, s));
   k_frame_begin_b<<<(n + 127) / 128, 128, 0, s>>>(t, n);
   mh_count_launches(1);
+  auto mark = [&](int st) {
+    if (timed) cudaEventRecord(b->sev[st], s);
+  };
   int r;
+  mark(MH_STAGE_PREPROCESS);
   if ((r = launch_batch_preprocess(t, n, s)) != MH_OK) return r;
+  mark(MH_STAGE_TV);
   if (tv_it > 0 && (r = launch_batch_tv(t, n, b->max_pixels, lambda, tv_it, s)) != MH_OK) return r;
+  mark(MH_STAGE_ALLOC);
   if ((r = launch_batch_alloc(t, n, b->alloc_tiles, s)) != MH_OK) return r;
+  mark(MH_STAGE_COLLECT);
   if ((r = launch_batch_collect(t, n, s)) != MH_OK) return r;
+  mark(MH_STAGE_PREDICT);
   if (b->has_psdf && (r = launch_batch_predict(t, n, s)) != MH_OK) return r;
+  mark(MH_STAGE_INTEGRATE);
   if (timed) cudaEventRecord(b->ev[0], s);
   if ((r = launch_batch_integrate(t, n, b->has_simple, b->has_psdf, kCtaCaps[b->tune.integrate_cta_per_sm], s)) !=
       MH_OK)
     return r;
   if (timed) cudaEventRecord(b->ev[1], s);
+  mark(MH_STAGE_MESH);
   if ((r = launch_batch_mesh(t, n, s)) != MH_OK) return r;
+  mark(MH_STAGE_GC);
   if ((r = launch_batch_gc_low_surfel(t, n, s)) != MH_OK) return r;
   if ((r = launch_batch_gc_recycle(t, n, 0, s)) != MH_OK) return r;
+  mark(MH_STAGE_RAYCAST);
   if (b->raycast) {
     if (timed) cudaEventRecord(b->ev[2], s);
     if ((r = launch_raycast_batch(t, n, b->ray_tiles(b->tune.ray_tile_shape, nullptr), b->tune.ray_tile_shape, s)) !=
@@ -123,6 +141,7 @@ static int enqueue(mh_batch *b, int p, bool host_depth, int tv_it, float lambda,
       return r;
     if (timed) cudaEventRecord(b->ev[3], s);
   }
+  mark(MH_STAGE_COUNT);
   if (b->has_simple) {
     if ((r = launch_batch_gc_starve(t, n, s)) != MH_OK) return r;
     if ((r = launch_batch_gc_recycle(t, n, 1, s)) != MH_OK) return r;
@@ -187,6 +206,8 @@ int mh_batch_create(mh_volume *const *volumes, int count, int raycast, mh_batch 
   }
   for (cudaEvent_t &e : b->ev)
     if (r == MH_OK && cudaEventCreate(&e) != cudaSuccess) r = MH_ERR_CUDA;
+  for (cudaEvent_t &e : b->sev)
+    if (r == MH_OK && cudaEventCreate(&e) != cudaSuccess) r = MH_ERR_CUDA;
   if (r == MH_OK && cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking) != cudaSuccess) r = MH_ERR_CUDA;
   if (r == MH_OK) {
     mh_sm_count();
@@ -247,7 +268,15 @@ int mh_batch_autotune(mh_batch *b, int trials) {
   if (!b || trials <= 0) return MH_ERR_INVALID;
   b->tune_left = trials * 9;
   b->tune_k = 0;
+  b->stage_steps = 0;
+  for (double &x : b->stage_ms) x = 0.0;
   for (int i = 0; i < 3; ++i) b->ray_ms[i] = b->int_ms[i] = 0.0, b->ray_cnt[i] = b->int_cnt[i] = 0;
+  return MH_OK;
+}
+
+int mh_batch_stage_times(mh_batch *b, double ms[MH_STAGE_COUNT]) {
+  if (!b || !ms) return MH_ERR_INVALID;
+  for (int st = 0; st < MH_STAGE_COUNT; ++st) ms[st] = b->stage_steps ? b->stage_ms[st] / b->stage_steps : -1.0;
   return MH_OK;
 }
 
@@ -356,6 +385,9 @@ int mh_batch_step(mh_batch *b, const float *const *depth, int depth_on_device, c
       b->ray_ms[b->tune.ray_tile_shape] += ms;
       b->ray_cnt[b->tune.ray_tile_shape] += 1;
     }
+    for (int st = 0; st < MH_STAGE_COUNT; ++st)
+      if (cudaEventElapsedTime(&ms, b->sev[st], b->sev[st + 1]) == cudaSuccess) b->stage_ms[st] += ms;
+    b->stage_steps += 1;
     b->tune_k += 1;
     if (--b->tune_left == 0) {
       int best_r = 0, best_i = 0;

@@ -77,8 +77,10 @@ __device__ __forceinline__ void mc_begin_body(const Dev &d) {
   d.ctr->cube_list_count = 0;
 }
 __global__ void k_mc_begin(Dev d) { mc_begin_body(d); }
+// one thread per scene (the body is a single-thread step)
 __global__ void k_mc_begin_b(const Scene *t, int n) {
-  each_scene(t, n, [&](const Scene &c) { mc_begin_body(c.d); });
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && t[i].active) mc_begin_body(t[i].d);
 }
 
 // Candidates the cube pass must tile: a block holding a mesh page, or one
@@ -115,8 +117,10 @@ __device__ __forceinline__ void mc_end_body(const Dev &d) {
   d.ctr->mesh_list_sum += (unsigned long long)d.ctr->mesh_list_count;
 }
 __global__ void k_mc_end(Dev d) { mc_end_body(d); }
+// one thread per scene (the body is a single-thread step)
 __global__ void k_mc_end_b(const Scene *t, int n) {
-  each_scene(t, n, [&](const Scene &c) { mc_end_body(c.d); });
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && t[i].active) mc_end_body(t[i].d);
 }
 
 // ------------------------------------------------------------------ pass 1
@@ -470,7 +474,7 @@ int launch_mesh(const Dev &d, cudaStream_t s) {
 
 int launch_batch_mesh(const Scene *t, int n, cudaStream_t s) {
   const int sms = mh_sm_count();
-  k_mc_begin_b<<<1, 1, 0, s>>>(t, n);
+  k_mc_begin_b<<<(n + 63) / 64, 64, 0, s>>>(t, n);
   k_mc_select_b<<<sms * 4, 256, 0, s>>>(t, n);
   k_mc_cubes_b<<<sms * 2, 512, 0, s>>>(t, n);
   k_mc_list_b<<<sms * 4, 256, 0, s>>>(t, n);
@@ -478,7 +482,7 @@ int launch_batch_mesh(const Scene *t, int n, cudaStream_t s) {
   k_mc_triangles_b<<<sms * 2, 512, 0, s>>>(t, n);
   k_mc_recycle_tri_b<<<sms * 8, 128, 0, s>>>(t, n);
   k_mc_recycle_vtx_b<<<sms * 8, 128, 0, s>>>(t, n);
-  k_mc_end_b<<<1, 1, 0, s>>>(t, n);
+  k_mc_end_b<<<(n + 63) / 64, 64, 0, s>>>(t, n);
   mh_count_launches(9);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }
