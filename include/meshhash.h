@@ -256,6 +256,39 @@ int mh_profile_read(mh_volume *v, double ms[MH_STAGE_COUNT], int calls[MH_STAGE_
 uint64_t mh_launch_count(void);
 
 /* Teschner hash of a block position (core/hash_table.h:259-269). */
+/* ------------------------------------------------------------------ gradients
+ * Differentiable raycast.  No reference counterpart (the reference's
+ * RayCaster::Cast, visualization/ray_caster.cu:16-224, is forward only).  The
+ * march is re-run with the forward's code, so its discrete decisions are the
+ * forward's; the derivative is taken through the two bracketing samples, the
+ * three regula-falsi steps and the gradient-based normal, i.e. it is the
+ * derivative of what mh_raycast computes.  Pose derivatives are for a left
+ * se(3) increment wTc <- exp(xi) wTc, xi = (tx, ty, tz, wx, wy, wz).
+ */
+/* For L = sum_pixels dL_ddepth * depth + dL_dnormal4.xyz . normal (device
+ * W x H float and W x H float4, either may be NULL): adds dL/dsdf into
+ * grad_sdf (device, value_capacity x 512 floats indexed like the volume's
+ * own voxel storage, NULL to skip; read it with mh_dump_block_field) and
+ * writes dL/dxi (host).  Synchronising. */
+int mh_raycast_backward(mh_volume *v, const float cTw[16], const float *dL_ddepth, const float *dL_dnormal4,
+                        float *grad_sdf, double dL_dxi[6], void *stream);
+/* Gauss-Newton normal equations of r = rendered depth - observed depth over
+ * the pixels with a hit, an observation (> 0, finite) and |r| < max_residual:
+ * J^T J (6 x 6 row-major), J^T r, sum r^2 and the pixel count, J = dr/dxi.
+ * obs_depth: device W x H, or NULL for the current frame's depth (needs equal
+ * sensor and raycast sizes).  Synchronising. */
+int mh_raycast_normal_equations(mh_volume *v, const float cTw[16], const float *obs_depth, float max_residual,
+                                double JtJ[36], double Jtr[6], double *cost, int *count, void *stream);
+/* Frame-to-model pose refinement: `iterations` Gauss-Newton steps on the
+ * depth residual above, starting from wTc (updated in place).  When a frame
+ * is set, its pose becomes the refined one.  final_cost / final_count (may be
+ * NULL): the residual at the returned pose. */
+int mh_refine_pose(mh_volume *v, const float *obs_depth, float wTc[16], int iterations, float max_residual,
+                   double *final_cost, int *final_count, void *stream);
+/* Like mh_dump_blocks for a caller's device field laid out like the voxel
+ * storage (value_capacity x 512 floats), e.g. the grad_sdf above. */
+int mh_dump_block_field(mh_volume *v, const float *field, int max_blocks, int32_t *pos, float *out, int *n_out);
+
 /* ------------------------------------------------------------------ batches
  * Many independent volumes (scenes) advanced together.  No reference
  * counterpart: the reference runs one MainEngine per process.  A step runs

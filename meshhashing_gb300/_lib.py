@@ -61,6 +61,11 @@ SIGNATURES = {
     "mh_profile_read": (i32, [MHV, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "mh_launch_count": (C.c_uint64, []),
     "mh_denoise_tv_static": (i32, [vp, vp, i32, i32, C.c_float, i32, vp]),
+    "mh_raycast_backward": (i32, [MHV, f32p, vp, vp, vp, C.POINTER(C.c_double), vp]),
+    "mh_raycast_normal_equations": (i32, [MHV, f32p, vp, C.c_float, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double), C.POINTER(C.c_int32), vp]),
+    "mh_refine_pose": (i32, [MHV, vp, f32p, i32, C.c_float, C.POINTER(C.c_double), C.POINTER(C.c_int32), vp]),
+    "mh_dump_block_field": (i32, [MHV, vp, i32, i32p, f32p, i32p]),
     "mh_batch_create": (i32, [C.POINTER(MHV), i32, i32, C.POINTER(vp)]),
     "mh_batch_destroy": (i32, [vp]),
     "mh_batch_step": (i32, [vp, C.POINTER(vp), i32, f32p, i32p, i32, C.c_float, i32, vp]),

@@ -370,6 +370,7 @@ int mh_volume_destroy(mh_volume *v) {
   for (cudaEvent_t e : v->ev_pool) cudaEventDestroy(e);
   for (void *p : v->allocs) cudaFree(p);
   if (v->scratch) cudaFree(v->scratch);
+  if (v->acc) cudaFree(v->acc);
   delete v;
   return MH_OK;
 }

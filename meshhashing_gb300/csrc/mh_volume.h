@@ -13,6 +13,7 @@ struct mh_volume {
   Dev d;
   float *tv = nullptr;
   float *rc_stage = nullptr;  // device staging for host raycast outputs
+  double *acc = nullptr;      // reduction target of the raycast gradients (allocated on first use)
   int *scratch = nullptr;     // device scratch for list operations
   size_t scratch_bytes = 0;
   FrameConst fc_host;

@@ -166,6 +166,50 @@ class Volume:
         self._c("mh_raycast", _ptr(m), _dev(depth_out), _dev(vertex_out), _dev(normal_out), 1, self.stream)
         return None
 
+    # ---------------------------------------------------------- gradients
+    def raycast_backward(self, cTw, dL_ddepth, dL_dnormal=None, grad_sdf=None):
+        """dL/dxi (left se(3) increment of wTc, translation first) for
+        L = sum dL_ddepth * depth + dL_dnormal[..., :3] . normal of the raycast
+        from cTw; dL_ddepth (H, W) and dL_dnormal (H, W, 4) are CUDA tensors or
+        device pointers.  grad_sdf (a CUDA tensor of value_capacity * 512
+        floats, laid out like the voxel storage) receives dL/dsdf added in."""
+        m = _f32(cTw).reshape(16)
+        xi = (C.c_double * 6)()
+        self._c("mh_raycast_backward", _ptr(m), _dev(dL_ddepth), _dev(dL_dnormal), _dev(grad_sdf), xi, self.stream)
+        return np.array(list(xi))
+
+    def normal_equations(self, cTw, obs_depth=None, max_residual: float = 0.1):
+        """(J^T J (6, 6), J^T r (6,), sum r^2, count) of r = rendered - observed
+        depth; obs_depth a CUDA tensor / device pointer, or None for the frame's."""
+        m = _f32(cTw).reshape(16)
+        A = (C.c_double * 36)()
+        b = (C.c_double * 6)()
+        cost = C.c_double()
+        cnt = C.c_int32()
+        self._c("mh_raycast_normal_equations", _ptr(m), _dev(obs_depth), C.c_float(max_residual), A, b,
+                C.byref(cost), C.byref(cnt), self.stream)
+        return np.array(list(A)).reshape(6, 6), np.array(list(b)), cost.value, cnt.value
+
+    def refine_pose(self, wTc, iterations: int = 10, obs_depth=None, max_residual: float = 0.1):
+        """Gauss-Newton frame-to-model refinement; returns (wTc, cost, count)."""
+        m = np.ascontiguousarray(np.asarray(wTc, np.float32).reshape(16))
+        cost = C.c_double()
+        cnt = C.c_int32()
+        self._c("mh_refine_pose", _dev(obs_depth), _ptr(m), int(iterations), C.c_float(max_residual), C.byref(cost),
+                C.byref(cnt), self.stream)
+        return m.reshape(4, 4), cost.value, cnt.value
+
+    def dump_block_field(self, field):
+        """(positions, rows) of a device per-voxel field laid out like the
+        voxel storage (e.g. the grad_sdf of raycast_backward)."""
+        n = C.c_int32()
+        self._c("mh_dump_block_field", _dev(field), 0, None, None, C.byref(n))
+        cnt = n.value
+        pos = np.zeros((max(cnt, 1), 3), np.int32)
+        out = np.zeros((max(cnt, 1), 512), np.float32)
+        self._c("mh_dump_block_field", _dev(field), cnt, _ptr(pos, C.c_int32), _ptr(out), C.byref(n))
+        return pos[:cnt], out[:cnt]
+
     def integrate_frame(self, depth, wTc, on_device: bool = False, tv_iterations: int = 0, tv_lambda: float = 0.1,
                         ray_depth=None, ray_vertex=None, ray_normal=None, outputs_on_device: bool = False):
         """One MainEngine frame: Mapping, Meshing, raycast, Recycle."""

@@ -1141,6 +1141,201 @@ template <class R> struct Vol {
     }
   }
 
+  // ---------------------------------------------------------- raycast backward
+  // Reverse-mode derivative of the raycast above (the library's
+  // mh_raycast_backward restated): along the recorded single-precision
+  // decisions, the depth m * cd.z is differentiated through the bracketing
+  // samples, the three regula-falsi steps and the gradient-based normal, for
+  // the voxel sdf values and a left se(3) increment of wTc (translation
+  // first).  Samples keep the hybrid cell choice of spatial_hyb.
+  struct SampD {
+    R s = 0;
+    V3<R> g{0, 0, 0};
+    int id[8];
+    int li[8];
+    R w[8];
+  };
+  bool spatial_d(V3<R> pos, V3<float> p32, SampD &o) const {
+    const float off = p.voxel_size;
+    V3<float> pc = mk(p32.x - 0.5f * off, p32.y - 0.5f * off, p32.z - 0.5f * off);
+    V3<float> q32 = p32 / off;
+    const float fl[3] = {std::floor(q32.x), std::floor(q32.y), std::floor(q32.z)};
+    const R vsr = (R)p.voxel_size;
+    const R ratio[3] = {pos.x / vsr - (R)fl[0], pos.y / vsr - (R)fl[1], pos.z / vsr - (R)fl[2]};
+    auto rnd = [&](float v) { float sg = v < 0.0f ? -1.0f : 1.0f; return f2i<float>(v / off + sg * 0.5f); };
+    R sum = 0, gx = 0, gy = 0, gz = 0;
+    for (int i = 0; i < 8; ++i) {
+      int mx = (i & 4) > 0, my = (i & 2) > 0, mz = (i & 1) > 0;
+      R rx = mx ? ratio[0] : (R)1 - ratio[0];
+      R ry = my ? ratio[1] : (R)1 - ratio[1];
+      R rz = mz ? ratio[2] : (R)1 - ratio[2];
+      I3 v{rnd(pc.x + (float)mx * off), rnd(pc.y + (float)my * off), rnd(pc.z + (float)mz * off)};
+      I3 bp = voxel_to_block(v);
+      int bid = find(bp.x, bp.y, bp.z);
+      if (bid < 0 || !blocks[bid]) return false;
+      int li = (v.x - bp.x * kB) + (v.y - bp.y * kB) * kB + (v.z - bp.z * kB) * kB * kB;
+      R val = (R)blocks[bid]->sdf[li];
+      sum += (rx * ry * rz) * val;
+      gx += (mx ? (R)1 : (R)-1) * ry * rz * val;
+      gy += (my ? (R)1 : (R)-1) * rx * rz * val;
+      gz += (mz ? (R)1 : (R)-1) * rx * ry * val;
+      o.id[i] = bid, o.li[i] = li, o.w[i] = rx * ry * rz;
+    }
+    o.s = sum;
+    o.g = mk(gx / vsr, gy / vsr, gz / vsr);
+    return true;
+  }
+  std::unordered_map<int, std::vector<double>> grad;
+  void scatter(const SampD &o, R a) {
+    if (a == (R)0) return;
+    for (int i = 0; i < 8; ++i) {
+      auto &g = grad[o.id[i]];
+      if (g.empty()) g.assign(kBV, 0.0);
+      g[o.li[i]] += (double)(a * o.w[i]);
+    }
+  }
+  static V3<R> cross(V3<R> a, V3<R> b) {
+    return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+  }
+  // dL_dD: W x H, dL_dN: W x H x 3 (may be null); xi receives dL/dxi
+  void raycast_backward(const M4<R> &cTw_, const float *dL_dD, const float *dL_dN, double xi[6]) {
+    grad.clear();
+    for (int k = 0; k < 6; ++k) xi[k] = 0;
+    M4<float> cf;
+    for (int i = 0; i < 16; ++i) cf.e[i] = (float)cTw_.e[i];
+    const M4<float> wf = inverse(cf);
+    const M4<R> wTc_ = sizeof(R) == 4 ? M4<R>{} : inverse(cTw_);
+    M4<R> wt;
+    for (int i = 0; i < 16; ++i) wt.e[i] = sizeof(R) == 4 ? (R)wf.e[i] : wTc_.e[i];
+    const int W = p.rc_width, H = p.rc_height;
+    const R vsr = (R)p.voxel_size;
+    for (int y = 0; y < H; ++y) {
+      for (int x = 0; x < W; ++x) {
+        const size_t pix = (size_t)y * W + x;
+        R aD = dL_dD ? (R)dL_dD[pix] : (R)0;
+        V3<R> aN = dL_dN ? mk((R)dL_dN[3 * pix], (R)dL_dN[3 * pix + 1], (R)dL_dN[3 * pix + 2]) : mk((R)0, (R)0, (R)0);
+        if (aD == (R)0 && aN.x == (R)0 && aN.y == (R)0 && aN.z == (R)0) continue;
+        Trace tr = march32(wf, x, y);
+        if (!tr.hit) continue;
+        const R rx = ((R)x - (R)p.rc_cx) / (R)p.rc_fx, ry = ((R)y - (R)p.rc_cy) / (R)p.rc_fy;
+        V3<R> cd = normalize(mk(rx, ry, (R)1));
+        V3<R> cam = wt.pt(mk((R)0, (R)0, (R)0));
+        V3<R> wd = normalize(wt.dir(cd));
+        V3<float> cdf = normalize(mk(((float)x - p.rc_cx) / p.rc_fx, ((float)y - p.rc_cy) / p.rc_fy, 1.0f));
+        V3<float> camf = wf.pt(mk(0.0f, 0.0f, 0.0f));
+        V3<float> wdf = normalize(wf.dir(cdf));
+        // forward along the recorded decisions
+        SampD S0, S1, Sm[3];
+        float l32 = tr.t0, r32 = tr.t1, ls32, rs32;
+        spatial_t<float>(camf + l32 * wdf, ls32);
+        spatial_t<float>(camf + r32 * wdf, rs32);
+        R l = tr.t0, r = tr.t1;
+        if (!spatial_d(cam + l * wd, camf + l32 * wdf, S0) || !spatial_d(cam + r * wd, camf + r32 * wdf, S1)) continue;
+        R ls = S0.s, rs = S1.s;
+        R L[3], Rr[3], LS[3], RS[3], M[3];
+        bool zero[3] = {false, false, false}, ok = true;
+        for (int k = 0; k < 3; ++k) {
+          L[k] = l, Rr[k] = r, LS[k] = ls, RS[k] = rs;
+          const float m32 = l32 + (ls32 / (ls32 - rs32)) * (r32 - l32);
+          const R m = l + (ls / (ls - rs)) * (r - l);
+          M[k] = m;
+          float ms32;
+          spatial_t<float>(camf + m32 * wdf, ms32);
+          if (!spatial_d(cam + m * wd, camf + m32 * wdf, Sm[k])) {
+            ok = false;
+            break;
+          }
+          R ms = Sm[k].s;
+          const bool left = (tr.side >> k) & 1;
+          if (left != ((double)(ls * ms) > 0.0)) ms = 0, zero[k] = true;
+          if (left) l = m, ls = ms, l32 = m32, ls32 = ms32;
+          else r = m, rs = ms, r32 = m32, rs32 = ms32;
+        }
+        if (!ok) continue;
+        const R m = M[2];
+        V3<R> a_cam = mk((R)0, (R)0, (R)0), a_wd = a_cam, a_w = a_cam;
+        R am = aD * cd.z;
+        if (dL_dN && (aN.x != (R)0 || aN.y != (R)0 || aN.z != (R)0)) {
+          V3<R> iso = cam + m * wd;
+          const R h = (R)0.5 * vsr;
+          SampD P[3], N[3];
+          bool gok = true;
+          for (int i = 0; i < 3 && gok; ++i) {
+            V3<R> dp = mk(i == 0 ? h : (R)0, i == 1 ? h : (R)0, i == 2 ? h : (R)0);
+            V3<R> a = iso - dp, b = iso + dp;
+            gok = spatial_d(a, mk((float)a.x, (float)a.y, (float)a.z), N[i]) &&
+                  spatial_d(b, mk((float)b.x, (float)b.y, (float)b.z), P[i]);
+          }
+          V3<R> g = mk((P[0].s - N[0].s) / vsr, (P[1].s - N[1].s) / vsr, (P[2].s - N[2].s) / vsr);
+          R len = std::sqrt(dot(g, g));
+          if (gok && len > (R)0) {
+            V3<R> u = g / len, nn = mk(-u.x, -u.y, -u.z);
+            const R *c = cTw_.e;
+            V3<R> a_nn = mk(c[0] * aN.x + c[4] * aN.y + c[8] * aN.z, c[1] * aN.x + c[5] * aN.y + c[9] * aN.z,
+                            c[2] * aN.x + c[6] * aN.y + c[10] * aN.z);
+            a_w = cross(a_nn, nn);
+            V3<R> a_u = mk(-a_nn.x, -a_nn.y, -a_nn.z);
+            R ua = dot(u, a_u);
+            R ag[3] = {(a_u.x - u.x * ua) / len, (a_u.y - u.y * ua) / len, (a_u.z - u.z * ua) / len};
+            V3<R> a_iso = mk((R)0, (R)0, (R)0);
+            for (int i = 0; i < 3; ++i) {
+              R ap = ag[i] / vsr, an = -ag[i] / vsr;
+              scatter(P[i], ap);
+              scatter(N[i], an);
+              a_iso = a_iso + ap * P[i].g + an * N[i].g;
+            }
+            a_cam = a_cam + a_iso;
+            a_wd = a_wd + m * a_iso;
+            am += dot(a_iso, wd);
+          }
+        }
+        R al = 0, ar = 0, als = 0, ars = 0;
+        for (int k = 2; k >= 0; --k) {
+          const bool left = (tr.side >> k) & 1;
+          R a_mk = (k == 2 ? am : (R)0) + (left ? al : ar);
+          R a_ms = left ? als : ars;
+          if (left) al = 0, als = 0;
+          else ar = 0, ars = 0;
+          if (zero[k]) a_ms = 0;   // the value was taken as exactly zero
+          scatter(Sm[k], a_ms);
+          V3<R> ap = a_ms * Sm[k].g;
+          a_cam = a_cam + ap;
+          a_wd = a_wd + M[k] * ap;
+          a_mk += dot(ap, wd);
+          const R den = LS[k] - RS[k], q = LS[k] / den, span = Rr[k] - L[k];
+          al += a_mk * ((R)1 - q);
+          ar += a_mk * q;
+          als += a_mk * span * (-RS[k]) / (den * den);
+          ars += a_mk * span * LS[k] / (den * den);
+        }
+        scatter(S0, als);
+        scatter(S1, ars);
+        V3<R> p0 = als * S0.g, p1 = ars * S1.g;
+        a_cam = a_cam + p0 + p1;
+        a_wd = a_wd + (R)tr.t0 * p0 + (R)tr.t1 * p1;
+        V3<R> aw = cross(cam, a_cam) + cross(wd, a_wd) + a_w;
+        xi[0] += a_cam.x, xi[1] += a_cam.y, xi[2] += a_cam.z;
+        xi[3] += aw.x, xi[4] += aw.y, xi[5] += aw.z;
+      }
+    }
+  }
+  // per pixel: hit, side, and the bits of t0, t1 of the single-precision trace
+  void trace_dump(const M4<R> &cTw_, int32_t *out) const {
+    M4<float> cf;
+    for (int i = 0; i < 16; ++i) cf.e[i] = (float)cTw_.e[i];
+    const M4<float> wf = inverse(cf);
+    const int W = p.rc_width, H = p.rc_height;
+#pragma omp parallel for schedule(dynamic, 2)
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        Trace tr = march32(wf, x, y);
+        int32_t *o = out + 4 * ((size_t)y * W + x);
+        o[0] = tr.hit, o[1] = tr.side;
+        memcpy(o + 2, &tr.t0, 4);
+        memcpy(o + 3, &tr.t1, 4);
+      }
+  }
+
   // ---------------------------------------------------------- GC
   // CollectLowSurfelBlocksKernel (mapping/recycle.cu:79-114)
   void gc_low_surfel() {
@@ -1568,6 +1763,45 @@ void orc_raycast(void *hp, const float *cTw, float *depth, float *vert, float *n
     decltype(vol->cTw) m;
     for (int i = 0; i < 16; ++i) m.e[i] = cTw[i];
     vol->raycast(m, depth, vert, norm);
+  });
+}
+
+void orc_raycast_backward(void *hp, const float *cTw, const float *dL_dD, const float *dL_dN, double *xi) {
+  OHandle *h = (OHandle *)hp;
+  DISPATCH(h, {
+    decltype(vol->cTw) m;
+    for (int i = 0; i < 16; ++i) m.e[i] = cTw[i];
+    vol->raycast_backward(m, dL_dD, dL_dN, xi);
+  });
+}
+
+// the gradient of the last backward, per block with any entry: positions and
+// 512 values each (returns the count; fills at most max_n)
+int orc_grad_blocks(void *hp, int max_n, int32_t *pos, double *out) {
+  OHandle *h = (OHandle *)hp;
+  int n = 0;
+  DISPATCH(h, {
+    std::vector<int> ids;
+    for (auto &kv : vol->grad) ids.push_back(kv.first);
+    std::sort(ids.begin(), ids.end());
+    for (int id : ids) {
+      if (n < max_n) {
+        const auto *b = vol->blocks[id].get();
+        if (pos) pos[3 * n] = b->x, pos[3 * n + 1] = b->y, pos[3 * n + 2] = b->z;
+        if (out) memcpy(out + (size_t)n * 512, vol->grad[id].data(), sizeof(double) * 512);
+      }
+      ++n;
+    }
+  });
+  return n;
+}
+
+void orc_trace(void *hp, const float *cTw, int32_t *out) {
+  OHandle *h = (OHandle *)hp;
+  DISPATCH(h, {
+    decltype(vol->cTw) m;
+    for (int i = 0; i < 16; ++i) m.e[i] = cTw[i];
+    vol->trace_dump(m, out);
   });
 }
 

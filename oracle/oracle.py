@@ -80,6 +80,10 @@ def lib():
         L.orc_denoise_tv.argtypes = [vp, C.c_float, C.c_int]
         L.orc_get_depth.argtypes = [vp, f32p]
         L.orc_debug_ray.argtypes = [vp, f32p, C.c_int, C.c_int, C.POINTER(C.c_double)]
+        L.orc_raycast_backward.argtypes = [vp, f32p, f32p, f32p, C.POINTER(C.c_double)]
+        L.orc_grad_blocks.restype = C.c_int
+        L.orc_grad_blocks.argtypes = [vp, C.c_int, i32p, C.POINTER(C.c_double)]
+        L.orc_trace.argtypes = [vp, f32p, i32p]
         L.orc_num_threads.restype = C.c_int
         L.orc_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -205,6 +209,34 @@ class Oracle:
         m = f32(cTw).reshape(16)
         self.L.orc_raycast(self.h, _p(m, C.c_float), _p(d, C.c_float), _p(v, C.c_float), _p(n, C.c_float))
         return d.reshape(H, W), v.reshape(H, W, 4), n.reshape(H, W, 4)
+
+    def raycast_backward(self, cTw, dL_ddepth, dL_dnormal=None):
+        """dL/dxi (6, left se(3) increment of wTc, translation first) for
+        L = sum dL_ddepth * depth + dL_dnormal . normal; the voxel gradient is
+        kept for grad_blocks()."""
+        a = f32(dL_ddepth).reshape(-1)
+        nrm = None if dL_dnormal is None else f32(dL_dnormal).reshape(-1)
+        xi = (C.c_double * 6)()
+        m = f32(cTw).reshape(16)
+        self.L.orc_raycast_backward(self.h, _p(m, C.c_float), _p(a, C.c_float), _p(nrm, C.c_float), xi)
+        return np.array(list(xi))
+
+    def grad_blocks(self):
+        """(positions (n, 3), dL/dsdf (n, 512)) of the last raycast_backward."""
+        n = self.L.orc_grad_blocks(self.h, 0, None, None)
+        pos = np.zeros((max(n, 1), 3), np.int32)
+        g = np.zeros((max(n, 1), 512), np.float64)
+        self.L.orc_grad_blocks(self.h, n, _p(pos, C.c_int32), g.ctypes.data_as(C.POINTER(C.c_double)))
+        return pos[:n], g[:n]
+
+    def trace(self, cTw):
+        """Per pixel (H, W, 4) int32: hit, regula-falsi sides, bits of t0 and t1
+        of the single-precision march (the raycast's discrete decisions)."""
+        W, H = self.params.rc_width, self.params.rc_height
+        out = np.zeros(W * H * 4, np.int32)
+        m = f32(cTw).reshape(16)
+        self.L.orc_trace(self.h, _p(m, C.c_float), _p(out, C.c_int32))
+        return out.reshape(H, W, 4)
 
     def debug_ray(self, cTw, x, y):
         out = (C.c_double * 16)()
