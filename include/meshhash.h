@@ -272,15 +272,22 @@ uint64_t mh_launch_count(void);
  * writes dL/dxi (host).  Synchronising. */
 int mh_raycast_backward(mh_volume *v, const float cTw[16], const float *dL_ddepth, const float *dL_dnormal4,
                         float *grad_sdf, double dL_dxi[6], void *stream);
-/* Gauss-Newton normal equations of r = rendered depth - observed depth over
- * the pixels with a hit, an observation (> 0, finite) and |r| < max_residual:
- * J^T J (6 x 6 row-major), J^T r, sum r^2 and the pixel count, J = dr/dxi.
- * obs_depth: device W x H, or NULL for the current frame's depth (needs equal
- * sensor and raycast sizes).  Synchronising. */
+/* Gauss-Newton normal equations of frame-to-model alignment, driven by the
+ * raycast: for every pixel with a hit, an observation (> 0, finite) and
+ * |rendered - observed depth| < max_residual, the observed point on the
+ * pixel's ray is compared with the tangent plane of the model at the hit
+ * (normal from central sdf differences 2.5 voxels either side, at most
+ * 0.8 truncation distances): r = n . (p_obs - p_hit),
+ * J = dr/dxi = [n, p_obs x n] (projective point-to-plane).  The exact
+ * derivative of the rendered depth (mh_raycast_backward) follows the
+ * millimetre-scale bumps of a fused surface and makes a poor Gauss-Newton
+ * model; the tangent plane does not.  Outputs J^T J (6 x 6 row-major),
+ * J^T r, sum r^2 and the pixel count. */
 int mh_raycast_normal_equations(mh_volume *v, const float cTw[16], const float *obs_depth, float max_residual,
                                 double JtJ[36], double Jtr[6], double *cost, int *count, void *stream);
 /* Frame-to-model pose refinement: `iterations` Gauss-Newton steps on the
- * depth residual above, starting from wTc (updated in place).  When a frame
+ * alignment above, starting from wTc (updated in place); the residual gate
+ * starts at 4 x max_residual and halves per step down to max_residual.  When a frame
  * is set, its pose becomes the refined one.  final_cost / final_count (may be
  * NULL): the residual at the returned pose. */
 int mh_refine_pose(mh_volume *v, const float *obs_depth, float wTc[16], int iterations, float max_residual,

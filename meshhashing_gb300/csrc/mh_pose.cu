@@ -8,6 +8,7 @@
 // of the same pixel, differentiated through the raycast itself (kernels in
 // mh_raycast.cu).  Pose perturbations are left se(3) increments
 // wTc <- exp(xi) wTc with xi = (v, w): translation first, then rotation.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -167,7 +168,12 @@ int mh_refine_pose(mh_volume *v, const float *obs_depth, float wTc[16], int iter
     for (int i = 0; i < 16; ++i) Tf[i] = (float)T[i];
     inverse4(Tf, cTw);
     double A[36], b[6];
-    int r = mh_raycast_normal_equations(v, cTw, obs_depth, max_residual, A, b, &cost, &count, stream);
+    // the residual gate opens at 4x max_residual and halves per iteration
+    // down to it: a start centimetres off keeps enough pixels, the last
+    // steps keep only close ones
+    const float gate = std::max(max_residual, 4.0f * max_residual * std::ldexp(1.0f, -it));
+    int r = mh_raycast_normal_equations(v, cTw, obs_depth, it == iterations ? max_residual : gate, A, b, &cost,
+                                        &count, stream);
     if (r != MH_OK) return r;
     if (it == iterations || count < 6) break;
     // Gauss-Newton step with a tiny Levenberg term for rank-deficient views

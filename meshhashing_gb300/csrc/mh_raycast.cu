@@ -145,8 +145,10 @@ __device__ __forceinline__ void miss_interval(const DevParams &p, int bx, int by
   slab(cam.z, wd.z, az + mz, az + side - mz, lo, hi);
 }
 
-__device__ __forceinline__ bool ray_gradient(const Dev &d, RayCache &c, F3 pos, F3 &g) {
-  const float h = 0.5f * d.p.voxel_size;
+// GetSpatialSDFGradient: central differences h = half a voxel either side
+// (spacing = 0.5); a wider spacing gives a smoother normal
+__device__ __forceinline__ bool ray_gradient(const Dev &d, RayCache &c, F3 pos, F3 &g, float spacing = 0.5f) {
+  const float h = spacing * d.p.voxel_size;
   const float vs = d.p.voxel_size;
   float gx = 0.0f, gy = 0.0f, gz = 0.0f;
 #pragma unroll 1
@@ -156,7 +158,7 @@ __device__ __forceinline__ bool ray_gradient(const Dev &d, RayCache &c, F3 pos, 
     float sn, sp;
     if (ray_sample(d, c, dm, sn) != RS_OK) return false;
     if (ray_sample(d, c, dp, sp) != RS_OK) return false;
-    const float gi = (sp - sn) / vs;
+    const float gi = (sp - sn) / (vs * (2.0f * spacing));
     gx = i == 0 ? gi : gx;
     gy = i == 1 ? gi : gy;
     gz = i == 2 ? gi : gz;
@@ -552,9 +554,12 @@ template <int NV> __device__ __forceinline__ void cta_accumulate(float (&v)[NV],
 
 // mode 0: accumulate dL/dsdf into grad (if given) and dL/dxi into acc[0..5]
 //         for L = sum dLdD * depth + dLdN . normal;
-// mode 1: Gauss-Newton normal equations of r = depth - obs over pixels with a
-//         hit, a valid observation and |r| < max_res: acc = [J^T J upper
-//         triangle (21), J^T r (6), sum r^2, count].
+// mode 1: Gauss-Newton normal equations of frame-to-model alignment over
+//         pixels with a hit, a valid observation and |depth - obs| < max_res:
+//         the observed point on the pixel's ray against the tangent plane of
+//         the model at the raycast hit (normal from the raycast's gradient),
+//         r = n . (p_obs - p_hit), J = [n, p_obs x n] for the left increment;
+//         acc = [J^T J upper triangle (21), J^T r (6), sum r^2, count].
 __global__ void __launch_bounds__(RC_TX *RC_TY) k_raycast_grad(Dev d, int mode, const float *dLdD, const float4 *dLdN,
                                                               float *grad, const float *obs, float max_res,
                                                               double *acc) {
@@ -598,7 +603,7 @@ __global__ void __launch_bounds__(RC_TX *RC_TY) k_raycast_grad(Dev d, int mode, 
       const RayTrace tr = ray_trace(d, c, cam, wd, t_min, t_max);
       if (tr.hit) {
         if (mode == 1) {
-          // the forward's depth, for the residual
+          // the forward's hit and normal
           float l = tr.t0, r = tr.t1, ls, rs_, m = 0.0f;
           ray_sample(d, c, f3(cam.x + l * wd.x, cam.y + l * wd.y, cam.z + l * wd.z), ls);
           ray_sample(d, c, f3(cam.x + r * wd.x, cam.y + r * wd.y, cam.z + r * wd.z), rs_);
@@ -609,13 +614,33 @@ __global__ void __launch_bounds__(RC_TX *RC_TY) k_raycast_grad(Dev d, int mode, 
             if ((tr.side >> k) & 1) l = m, ls = ms;
             else r = m, rs_ = ms;
           }
-          res = m * cd.z - obs[pix];
-          want = fabsf(res) < max_res;
-          aD = 1.0f;
+          const float o = obs[pix];
+          const F3 pm = f3(cam.x + m * wd.x, cam.y + m * wd.y, cam.z + m * wd.z);
+          // the normal of the alignment is taken 2.5 voxels either side
+          // (inside the truncation band): the half-voxel normal of the
+          // rendered image follows the noise of the fused surface, and a
+          // noisy normal in J shrinks every Gauss-Newton step (measured: from
+          // 2-8 cm / 1-2.5 degree starts, 8 iterations reached 15-90 mm with
+          // the half-voxel normal and 1-3 mm on three of four with this one)
+          const float spacing = fminf(2.5f, 0.8f * p.truncation_distance / p.voxel_size);
+          F3 g;
+          if (fabsf(m * cd.z - o) < max_res && ray_gradient(d, c, pm, g, spacing)) {
+            const float gl = sqrtf(dot3(g, g));
+            if (gl > 0.0f) {
+              // projective point-to-plane: the observed point on the same ray
+              // against the tangent plane of the model at the hit
+              const F3 n = f3(g.x / gl, g.y / gl, g.z / gl);
+              const float to = o / cd.z;
+              const F3 po = f3(cam.x + to * wd.x, cam.y + to * wd.y, cam.z + to * wd.z);
+              res = dot3(n, f3(po.x - pm.x, po.y - pm.y, po.z - pm.z));
+              av = n;
+              aw = cross3(po, n);
+              used = true;
+            }
+          }
+        } else {
+          used = pixel_backward(d, c, cTw, cam, wd, cd.z, tr, aD, aN, dLdN != nullptr, grad, av, aw);
         }
-        if (want)
-          used = pixel_backward(d, c, cTw, cam, wd, cd.z, tr, aD, aN, mode == 0 && dLdN != nullptr,
-                                mode == 0 ? grad : nullptr, av, aw);
       }
     }
   }
