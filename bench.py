@@ -194,6 +194,43 @@ def batch_params(spec, frames_run):
                              overflow_capacity=max(buckets // 4, 1024), mesh_page_capacity=max(cap // 64, 2048))
 
 
+def run_pose_refinement(vol, frames, poses, W, H, iterations=10):
+    """Frame-to-model refinement on the fused map: each frame starts from its
+    true pose perturbed by sigma 1 degree / 2 cm per axis (seeded) and runs
+    `iterations` Gauss-Newton steps (mh_refine_pose); plus one full-frame
+    raycast backward with voxel gradients."""
+    import torch
+    from meshhashing_gb300.pose import left_update, pose_error
+    rng = np.random.default_rng(77)
+    start, final, ms = [], [], []
+    for d, T in zip(frames, poses):
+        T_true = np.asarray(T, np.float64)
+        xi = np.concatenate([rng.standard_normal(3) * 0.02, rng.standard_normal(3) * np.radians(1.0)])
+        T0 = left_update(T_true, xi)
+        vol.set_frame(d, T0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        T_ref, cost, count = vol.refine_pose(T0, iterations=iterations, max_residual=0.05)
+        ms.append((time.perf_counter() - t0) * 1000.0)
+        start.append(pose_error(T0, T_true))
+        final.append(pose_error(T_ref, T_true))
+    cTw = np.linalg.inv(np.asarray(poses[0], np.float64)).astype(np.float32)
+    dl = torch.randn((H, W), generator=torch.Generator().manual_seed(3)).cuda()
+    grad = torch.zeros(vol.params.value_capacity * 512, dtype=torch.float32, device="cuda")
+    vol.raycast_backward(cTw, dl, None, grad)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    vol.raycast_backward(cTw, dl, None, grad)
+    bw_ms = (time.perf_counter() - t0) * 1000.0
+    med = lambda xs, k: float(np.median([x[k] for x in xs]))
+    return {"frames": len(frames), "iterations": iterations, "ms_per_frame": float(np.median(ms)),
+            "start_error": {"mm": med(start, 0) * 1000.0, "deg": med(start, 1)},
+            "final_error": {"mm": med(final, 0) * 1000.0, "deg": med(final, 1)},
+            "final_error_max": {"mm": max(x[0] for x in final) * 1000.0, "deg": max(x[1] for x in final)},
+            "raycast_backward_ms": bw_ms,
+            "note": "median over frames; perturbation sigma 1 deg / 2 cm per axis; PSDF map of this run"}
+
+
 def run_batched(specs, frames, poses, P, W, K):
     """Aggregate frames/s of the scenes advanced one after another with the
     plain per-frame chain, then (same volumes, reset) as one batch: one launch
@@ -341,7 +378,8 @@ def main():
         return
 
     K, W, P = args.steps, args.warmup, args.prefuse
-    n_total = P + W + 3 * K
+    R_POSE = 8
+    n_total = P + W + 3 * K + R_POSE
     # frames are rendered in a spawn pool before any CUDA call
     frames, poses = gen_frames(list(range(n_total)), max(500, n_total))
     cpu_frames = None
@@ -443,6 +481,15 @@ def main():
     per_launch_ms = stage_ms[dom] / calls
     alg = bytes_per_launch(dom, nb, px, rpx, vwork, **counts)
     achieved = alg / (per_launch_ms / 1000.0) / 1e9
+    # DRAM bytes per launch measured by ncu (dram__bytes_read.sum + _write.sum)
+    # on this workload at 454,148 candidate blocks, scaled by this run's count
+    NCU_TRAFFIC = {"raycast": (392.1e6, 454148.0), "integrate": (3.04e9, 454148.0)}
+    traffic, traffic_src = None, None
+    if dom in NCU_TRAFFIC:
+        b0, n0 = NCU_TRAFFIC[dom]
+        traffic = b0 * nb / n0
+        traffic_src = ("ncu DRAM read+write of one launch at %d candidate blocks (frames 44-45 of this workload), "
+                       "scaled by candidate blocks" % int(n0))
     stages = {}
     for k, (t_ms, c) in prof.items():
         if c:
@@ -450,6 +497,7 @@ def main():
             gbs = b / ((t_ms / c) / 1000.0) / 1e9 if t_ms > 0 else None
             stages[k] = {"ms_per_frame": t_ms / K, "gbs": gbs, "frac": (gbs / peak) if gbs else None}
 
+    pose = run_pose_refinement(vol, frames[P + W + 3 * K:], poses[P + W + 3 * K:], Ww, Hh)
     vol.close()
     batched = None
     if bspecs:
@@ -477,13 +525,14 @@ def main():
                        "d2h_bytes_per_step": rpx * 4},
                "gpu_launches": int(launches),
                "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                            "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                            "bytes_per_launch": alg},
+                            "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                            "bytes_per_launch": alg, "traffic_source": traffic_src},
                "stages": stages,
                "blocks": {"candidates_per_frame": nb, "vertices_per_frame": vwork, **counts,
                           "allocated": s2["blocks_allocated"], "mesh_pages": s2["mesh_pages_used"],
                           "error": s2["error"]},
                "clocks": clocks,
+               "pose_refinement": pose,
                "batched": batched,
                "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
