@@ -308,6 +308,62 @@ def run_batched(specs, frames, poses, P, W, K):
             "scenes_with_error": {"plain": int(err_plain), "batched": int(err_batch)}}
 
 
+# ---------------------------------------------------------------- streaming
+STREAM_FRAMES = 300
+
+
+def _stream_job(i):
+    from meshhashing_gb300 import scene
+    wl = scene.floor_plan(2000)
+    return wl.frame(i), wl.pose(i)
+
+
+def gen_stream_frames(n):
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(min(os.cpu_count() or 4, 16)) as pool:
+        out = pool.map(_stream_job, list(range(n)), chunksize=2)
+    return [o[0] for o in out], [o[1] for o in out]
+
+
+def run_stream(frames, poses):
+    """Large-scene streaming: the first frames of the 2000-frame walk through
+    the 12 x 10 x 3 m floor plan (640x480, 5 mm voxels, PSDF, 2^22 buckets),
+    the full MainEngine chain with a raycast every frame."""
+    import torch
+    from meshhashing_gb300 import Volume, config, scene
+    wl = scene.floor_plan(2000)
+    p = config.params_for(wl, voxel_size=0.005, truncation=0.015, value_capacity=1 << 22, bucket_count=1 << 22,
+                          max_vertex_count=1 << 23, max_triangle_count=1 << 23, overflow_capacity=1 << 20,
+                          mesh_page_capacity=1 << 17)
+    vol = Volume(p)
+    dev = torch.from_numpy(np.stack(frames)).cuda()
+    rd = torch.empty((p.height, p.width), dtype=torch.float32, device="cuda")
+    rn = torch.empty((p.height, p.width, 4), dtype=torch.float32, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    peak = 0
+    torch.cuda.synchronize()
+    e0.record()
+    for i in range(len(frames)):
+        vol.integrate_frame(dev[i], poses[i], on_device=True, tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA,
+                            ray_depth=rd, ray_normal=rn, outputs_on_device=True)
+        if i % 50 == 49:
+            peak = max(peak, vol.stats()["blocks_allocated"])
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    s = vol.stats()
+    vol.close()
+    return {"workload": "floor plan 12x10x3 m, 6 rooms, 40 primitives; 640x480 walk at 0.4 m/s, 5 mm voxels, "
+                        "PSDF, 2^22 buckets, TV %d it, raycast every frame" % TV_ITERS,
+            "frames": len(frames), "value": len(frames) / (ms / 1000.0), "unit": "frames/s",
+            "ms_per_frame": ms / len(frames), "blocks_allocated": s["blocks_allocated"], "blocks_peak": int(peak),
+            "gc_freed_blocks": s["gc_freed_blocks"], "triangles": s["triangles_allocated"],
+            "vertices": s["vertices_allocated"], "candidates_per_frame": s["candidate_sum"] / max(s["mesh_passes"], 1),
+            "error": s["error"], "dropped_inserts": s["dropped_inserts"],
+            "note": "frames 0..%d of the 2000-frame walk, the map growing from empty; the stats() reads "
+                    "every 50 frames are inside the timed region" % (len(frames) - 1)}
+
+
 def run_cpu_baseline(params, frames, poses, threads=None):
     """FP64 oracle on all host threads, from an empty volume."""
     from oracle import oracle as O
@@ -365,6 +421,8 @@ def main():
     ap.add_argument("--batch-scenes", type=int, default=64,
                     help="scenes of the batched-vs-plain measurement (0: skip it)")
     ap.add_argument("--batch-steps", type=int, default=5)
+    ap.add_argument("--stream-frames", type=int, default=STREAM_FRAMES,
+                    help="frames of the floor-plan streaming measurement (0: skip it)")
     ap.add_argument("--capacity-log2", type=int, default=21,
                     help="block pool size (2^n blocks); smaller values for profiler captures")
     args = ap.parse_args()
@@ -389,6 +447,7 @@ def main():
     bspecs = batch_specs(args.batch_scenes) if (args.batch_scenes > 0 and world == 1) else []
     BP, BW, BK = 9, 3, args.batch_steps
     bframes = gen_batch_frames(bspecs, BP + BW + BK) if bspecs else None
+    sframes = gen_stream_frames(args.stream_frames) if (args.stream_frames > 0 and world == 1) else None
 
     import torch
     torch.cuda.set_device(local)
@@ -505,6 +564,7 @@ def main():
         small = [k for k, sp in enumerate(bspecs) if sp["width"] < 640]
         batched["below_640x480"] = run_batched([bspecs[k] for k in small], [bframes[0][k] for k in small],
                                                [bframes[1][k] for k in small], BP, BW, BK)
+    stream = run_stream(*sframes) if sframes else None
 
     cpu = None
     if cpu_frames is not None:
@@ -534,6 +594,7 @@ def main():
                "clocks": clocks,
                "pose_refinement": pose,
                "batched": batched,
+               "stream": stream,
                "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     if world > 1:

@@ -239,6 +239,113 @@ def spline_trajectory(n: int, seed: int, fps: float = 30.0, vmax: float = 0.5) -
     return poses
 
 
+# ---------------------------------------------------------------- floor plan
+
+PLAN_LO = np.array([-6.0, -5.0, 0.0])
+PLAN_HI = np.array([6.0, 5.0, 3.0])
+_WALL = 0.05          # half thickness of interior walls
+_DOOR_W, _DOOR_H = 0.5, 2.1   # half width, height of a doorway
+
+
+def _room_centre(i: int, j: int) -> np.ndarray:
+    return np.array([-4.0 + 4.0 * i, -2.5 + 5.0 * j, 0.0])
+
+
+def _wall_slabs():
+    """Interior walls of the 3 x 2 room grid as solid slabs, with a doorway
+    on every room-centre line (x = -2, 2 at y = -2.5, 2.5; y = 0 at x = -4, 0, 4)."""
+    slabs = []
+
+    def wall_x(x, doors):
+        # wall at x spanning y in [-5, 5], doors centred at `doors`
+        edges = [-5.0] + [e for c in sorted(doors) for e in (c - _DOOR_W, c + _DOOR_W)] + [5.0]
+        for a, b in zip(edges[0::2], edges[1::2]):
+            slabs.append([x - _WALL, a, 0.0, x + _WALL, b, 3.0])
+        for c in doors:
+            slabs.append([x - _WALL, c - _DOOR_W, _DOOR_H, x + _WALL, c + _DOOR_W, 3.0])
+
+    def wall_y(y, doors):
+        edges = [-6.0] + [e for c in sorted(doors) for e in (c - _DOOR_W, c + _DOOR_W)] + [6.0]
+        for a, b in zip(edges[0::2], edges[1::2]):
+            slabs.append([a, y - _WALL, 0.0, b, y + _WALL, 3.0])
+        for c in doors:
+            slabs.append([c - _DOOR_W, y - _WALL, _DOOR_H, c + _DOOR_W, y + _WALL, 3.0])
+
+    wall_x(-2.0, [-2.5, 2.5])
+    wall_x(2.0, [-2.5, 2.5])
+    wall_y(0.0, [-4.0, 0.0, 4.0])
+    return slabs
+
+
+# the walk: room centres in loop order (through the doorways between them)
+_LOOP = [(0, 0), (1, 0), (2, 0), (2, 1), (1, 1), (0, 1), (0, 0)]
+
+
+def _dist_to_path(x: float, y: float) -> float:
+    best = np.inf
+    for (i0, j0), (i1, j1) in zip(_LOOP[:-1], _LOOP[1:]):
+        a, b = _room_centre(i0, j0)[:2], _room_centre(i1, j1)[:2]
+        ab = b - a
+        t = np.clip(np.dot(np.array([x, y]) - a, ab) / np.dot(ab, ab), 0.0, 1.0)
+        best = min(best, float(np.linalg.norm(np.array([x, y]) - (a + t * ab))))
+    return best
+
+
+def floor_plan_scene(seed: int = 0, n_primitives: int = 40) -> Scene:
+    """12 x 10 x 3 m floor plan: 6 rooms (3 x 2) separated by walls with
+    doorways, and n_primitives random boxes and spheres inside the rooms,
+    clear of the walls and of the walking path."""
+    rng = np.random.default_rng(5000 + seed)
+    sph, boxes = [], list(_wall_slabs())
+    while len(sph) + len(boxes) - len(_wall_slabs()) < n_primitives:
+        size = rng.uniform(0.1, 0.4)
+        i, j = int(rng.integers(0, 3)), int(rng.integers(0, 2))
+        c = _room_centre(i, j)
+        x = c[0] + rng.uniform(-2.0 + _WALL + size + 0.2, 2.0 - _WALL - size - 0.2)
+        y = c[1] + rng.uniform(-2.5 + _WALL + size + 0.2, 2.5 - _WALL - size - 0.2)
+        if _dist_to_path(x, y) < size + 0.7:
+            continue
+        z = rng.uniform(size, 2.6 - size) if rng.random() < 0.4 else size
+        if rng.random() < 0.5:
+            sph.append([x, y, z, size])
+        else:
+            boxes.append([x - size, y - size, z - size, x + size, y + size, z + size])
+    return Scene(PLAN_LO.copy(), PLAN_HI.copy(), np.array(sph, np.float64).reshape(-1, 4),
+                 np.array(boxes, np.float64).reshape(-1, 6))
+
+
+def floor_plan_walk(n: int, seed: int = 0, fps: float = 30.0, speed: float = 0.4) -> List[np.ndarray]:
+    """n poses walking the room loop at `speed` m/s (<= 0.5), eye height about
+    1.5 m, heading along the path (smoothed over +-0.6 m of arc) with a slow
+    look-around of +-35 degrees and a slight downward pitch."""
+    rng = np.random.default_rng(6000 + seed)
+    pts = [_room_centre(i, j)[:2] for i, j in _LOOP]
+    seg = [np.linalg.norm(b - a) for a, b in zip(pts[:-1], pts[1:])]
+    total = float(sum(seg))
+
+    def at(sarc):
+        sarc = sarc % total
+        for (a, b), L in zip(zip(pts[:-1], pts[1:]), seg):
+            if sarc <= L:
+                return a + (b - a) * (sarc / L)
+            sarc -= L
+        return pts[-1]
+
+    ph1, ph2 = rng.uniform(0, 2 * math.pi, 2)
+    poses = []
+    for k in range(n):
+        t = k / fps
+        sarc = speed * t + 0.3
+        p = at(sarc)
+        dvec = at(sarc + 0.6) - at(sarc - 0.6)
+        yaw = math.atan2(dvec[1], dvec[0]) + math.radians(35.0) * math.sin(2 * math.pi * t / 6.0 + ph1)
+        z = 1.5 + 0.08 * math.sin(2 * math.pi * t / 4.0 + ph2)
+        pos = np.array([p[0], p[1], z])
+        target = pos + np.array([math.cos(yaw), math.sin(yaw), -0.18])
+        poses.append(look_at(pos, target, roll=0.03 * math.sin(2 * math.pi * t / 5.0)))
+    return poses
+
+
 # ---------------------------------------------------------------- workloads
 
 @dataclasses.dataclass
@@ -275,3 +382,12 @@ def full_spline(n_frames: int = 500, seed: int = 0, width: int = 640, height: in
                     spline_trajectory(n_frames, seed),
                     dict(sigma_coef=0.0012, outlier_frac=0.05, outlier_range=(0.3, 5.0),
                          zero_frac=0.02), seed)
+
+
+def floor_plan(n_frames: int = 2000, seed: int = 0, width: int = 640, height: int = 480) -> Workload:
+    """Large-scene streaming case: the 12 x 10 x 3 m floor plan walked at
+    0.4 m/s, 640x480 (fx = fy = 525 at that width), noise as full_spline."""
+    s = width / 640.0
+    cam = Camera(width, height, 525.0 * s, 525.0 * s, (width - 1) / 2.0, (height - 1) / 2.0)
+    return Workload(f"floorplan{width}_walk", floor_plan_scene(seed), cam, floor_plan_walk(n_frames, seed),
+                    dict(sigma_coef=0.0012, outlier_frac=0.05, outlier_range=(0.3, 5.0), zero_frac=0.02), seed)
