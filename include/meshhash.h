@@ -256,6 +256,18 @@ int mh_profile_read(mh_volume *v, double ms[MH_STAGE_COUNT], int calls[MH_STAGE_
 uint64_t mh_launch_count(void);
 
 /* Teschner hash of a block position (core/hash_table.h:259-269). */
+/* Dense copy of the mesh (CompressMesh, visualization/compress_mesh.cu:10-172):
+ * the vertices referenced by live triangles (position and normal, 3 floats
+ * each) and the triangles with their indices remapped, in pool order, so the
+ * result does not vary between calls.  At most max_* entries are written
+ * (host or device buffers per out_on_device); n_* receive the totals.
+ * Allocates and frees its device staging; synchronising. */
+int mh_mesh_compact(mh_volume *v, int max_vertices, float *positions3, float *normals3, int max_triangles,
+                    int32_t *triangles3, int *n_vertices, int *n_triangles, int out_on_device, void *stream);
+/* The dense mesh as a binary little-endian PLY file (io/mesh_writer.cc:14-150
+ * writes the reference's): float x y z nx ny nz per vertex, uchar-int lists. */
+int mh_write_ply(mh_volume *v, const char *path);
+
 /* ------------------------------------------------------------------ gradients
  * Differentiable raycast.  No reference counterpart (the reference's
  * RayCaster::Cast, visualization/ray_caster.cu:16-224, is forward only).  The

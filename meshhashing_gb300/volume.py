@@ -166,6 +166,23 @@ class Volume:
         self._c("mh_raycast", _ptr(m), _dev(depth_out), _dev(vertex_out), _dev(normal_out), 1, self.stream)
         return None
 
+    # ---------------------------------------------------------- mesh export
+    def compact_mesh(self):
+        """(positions (V, 3), normals (V, 3), triangles (T, 3) int32): the
+        dense mesh in pool order."""
+        nv, nt = C.c_int32(), C.c_int32()
+        self._c("mh_mesh_compact", 0, None, None, 0, None, C.byref(nv), C.byref(nt), 0, self.stream)
+        V, T = nv.value, nt.value
+        pos = np.zeros((max(V, 1), 3), np.float32)
+        nrm = np.zeros((max(V, 1), 3), np.float32)
+        tri = np.zeros((max(T, 1), 3), np.int32)
+        self._c("mh_mesh_compact", V, pos.ctypes.data_as(C.c_void_p), nrm.ctypes.data_as(C.c_void_p), T,
+                tri.ctypes.data_as(C.c_void_p), C.byref(nv), C.byref(nt), 0, self.stream)
+        return pos[:V], nrm[:V], tri[:T]
+
+    def write_ply(self, path: str):
+        self._c("mh_write_ply", str(path).encode())
+
     # ---------------------------------------------------------- gradients
     def raycast_backward(self, cTw, dL_ddepth, dL_dnormal=None, grad_sdf=None):
         """dL/dxi (left se(3) increment of wTc, translation first) for
