@@ -268,6 +268,16 @@ int mh_mesh_compact(mh_volume *v, int max_vertices, float *positions3, float *no
  * writes the reference's): float x y z nx ny nz per vertex, uchar-int lists. */
 int mh_write_ply(mh_volume *v, const char *path);
 
+/* Block checkpoint (the reference's block recording,
+ * engine/logging_engine.cc:101-233): every allocated block's position and
+ * voxel fields (sdf and weight; with the Bayesian update also a and b) in one
+ * binary file, streamed in chunks.  Synchronising. */
+int mh_save_volume(mh_volume *v, const char *path);
+/* Resume: insert the file's blocks (the voxel size must match; existing blocks
+ * at the same positions are overwritten).  The mesh is re-extracted by the
+ * next mesh pass (e.g. mh_collect_all + mh_mesh).  n_blocks may be NULL. */
+int mh_load_volume(mh_volume *v, const char *path, int *n_blocks);
+
 /* ------------------------------------------------------------------ gradients
  * Differentiable raycast.  No reference counterpart (the reference's
  * RayCaster::Cast, visualization/ray_caster.cu:16-224, is forward only).  The

@@ -68,6 +68,8 @@ SIGNATURES = {
     "mh_dump_block_field": (i32, [MHV, vp, i32, i32p, f32p, i32p]),
     "mh_mesh_compact": (i32, [MHV, i32, vp, vp, i32, vp, i32p, i32p, i32, vp]),
     "mh_write_ply": (i32, [MHV, C.c_char_p]),
+    "mh_save_volume": (i32, [MHV, C.c_char_p]),
+    "mh_load_volume": (i32, [MHV, C.c_char_p, i32p]),
     "mh_batch_create": (i32, [C.POINTER(MHV), i32, i32, C.POINTER(vp)]),
     "mh_batch_destroy": (i32, [vp]),
     "mh_batch_step": (i32, [vp, C.POINTER(vp), i32, f32p, i32p, i32, C.c_float, i32, vp]),

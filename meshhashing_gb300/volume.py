@@ -183,6 +183,16 @@ class Volume:
     def write_ply(self, path: str):
         self._c("mh_write_ply", str(path).encode())
 
+    def save(self, path: str):
+        """Block checkpoint (positions and voxel fields) to a file."""
+        self._c("mh_save_volume", str(path).encode())
+
+    def load(self, path: str) -> int:
+        """Insert a checkpoint's blocks; returns their count."""
+        n = C.c_int32()
+        self._c("mh_load_volume", str(path).encode(), C.byref(n))
+        return n.value
+
     # ---------------------------------------------------------- gradients
     def raycast_backward(self, cTw, dL_ddepth, dL_dnormal=None, grad_sdf=None):
         """dL/dxi (left se(3) increment of wTc, translation first) for
