@@ -70,6 +70,8 @@ SIGNATURES = {
     "mh_write_ply": (i32, [MHV, C.c_char_p]),
     "mh_save_volume": (i32, [MHV, C.c_char_p]),
     "mh_load_volume": (i32, [MHV, C.c_char_p, i32p]),
+    "mh_huber_tv_init": (i32, [MHV, vp]),
+    "mh_huber_tv_iterate": (i32, [MHV, C.c_float, C.c_float, C.c_float, i32, C.POINTER(C.c_double), vp]),
     "mh_batch_create": (i32, [C.POINTER(MHV), i32, i32, C.POINTER(vp)]),
     "mh_batch_destroy": (i32, [vp]),
     "mh_batch_step": (i32, [vp, C.POINTER(vp), i32, f32p, i32p, i32, C.c_float, i32, vp]),

@@ -21,7 +21,7 @@ OBJ = os.path.join(HERE, "_build")
 SOURCES = ["mh_volume.cu", "mh_alloc.cu", "mh_integrate.cu", "mh_mesh.cu", "mh_raycast.cu", "mh_gc.cu",
            "mh_tv.cu",
            "mh_batch.cu", "mh_pose.cu",
-           "mh_compact.cu", "mh_io.cu"]
+           "mh_compact.cu", "mh_io.cu", "mh_huber.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
          "--expt-relaxed-constexpr"]

@@ -371,6 +371,7 @@ int mh_volume_destroy(mh_volume *v) {
   for (void *p : v->allocs) cudaFree(p);
   if (v->scratch) cudaFree(v->scratch);
   if (v->acc) cudaFree(v->acc);
+  mh_pd_free(v);
   delete v;
   return MH_OK;
 }

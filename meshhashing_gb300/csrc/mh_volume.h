@@ -8,12 +8,15 @@
 
 #include "mh_internal.cuh"
 
+struct mh_pd_state;
+
 struct mh_volume {
   mh_params hp;
   Dev d;
   float *tv = nullptr;
   float *rc_stage = nullptr;  // device staging for host raycast outputs
   double *acc = nullptr;      // reduction target of the raycast gradients (allocated on first use)
+  mh_pd_state *pd = nullptr;  // Huber-TV state (allocated on first use)
   int *scratch = nullptr;     // device scratch for list operations
   size_t scratch_bytes = 0;
   FrameConst fc_host;
@@ -39,3 +42,5 @@ struct mh_volume {
 // 4x4 inverse by cofactors with the term order of float4x4::getInverse
 // (extern/cuda/matrix.h:964-1086)
 void inverse4(const float *m, float *out);
+// releases the Huber-TV state of a volume (mh_huber.cu)
+void mh_pd_free(mh_volume *v);

@@ -193,6 +193,20 @@ class Volume:
         self._c("mh_load_volume", str(path).encode(), C.byref(n))
         return n.value
 
+    # ---------------------------------------------------------- Huber-TV
+    def huber_tv_init(self):
+        """Record sdf0 and the data weights over the current candidate blocks
+        (PrimalDualInit, optimize/primal_dual.cu:15-40)."""
+        self._c("mh_huber_tv_init", self.stream)
+
+    def huber_tv_iterate(self, lam: float, sigma: float, tau: float, iterations: int = 1) -> np.ndarray:
+        """Primal-dual Huber-TV steps on the sdf in place (PrimalDualIterate,
+        optimize/primal_dual.cu:176-223).  Returns [lam/2 data + tv, data, tv]
+        of the last iteration's dual pass."""
+        e = (C.c_double * 3)()
+        self._c("mh_huber_tv_iterate", float(lam), float(sigma), float(tau), int(iterations), e, self.stream)
+        return np.array(list(e))
+
     # ---------------------------------------------------------- gradients
     def raycast_backward(self, cTw, dL_ddepth, dL_dnormal=None, grad_sdf=None):
         """dL/dxi (left se(3) increment of wTc, translation first) for

@@ -705,6 +705,137 @@ template <class R> struct Vol {
     }
   }
 
+  // ---------------------------------------------------------- Huber-TV
+  // Primal-dual state of PrimalDualVariables (core/voxel.h:62-82), kept for
+  // the blocks that were candidates at the last init; other blocks read as
+  // unmasked.
+  struct PDB {
+    R sdf0[kBV], bar[kBV], w[kBV], p[kBV][3];
+    bool mask[kBV];
+  };
+  std::unordered_map<int, std::unique_ptr<PDB>> pd;
+  double pd_err[2] = {0, 0};
+
+  // block id and local index of voxel v, -1 when its block does not exist
+  int voxel_id(I3 v, int &li) const {
+    I3 bp = voxel_to_block(v);
+    int id = find(bp.x, bp.y, bp.z);
+    if (id < 0 || !blocks[id]) return -1;
+    li = (v.x - bp.x * kB) + (v.y - bp.y * kB) * kB + (v.z - bp.z * kB) * kB * kB;
+    return id;
+  }
+  static I3 step(I3 v, int k, int s) { return I3{v.x + (k == 0) * s, v.y + (k == 1) * s, v.z + (k == 2) * s}; }
+  // neighbour usable by the masked queries (primal_dual_query.h:90-234):
+  // block exists, voxel observed, mask set
+  const PDB *pd_usable(I3 v, int &li) const {
+    int id = voxel_id(v, li);
+    if (id < 0 || blocks[id]->w[li] < (R)1e-6f) return nullptr;
+    auto it = pd.find(id);
+    if (it == pd.end() || !it->second->mask[li]) return nullptr;
+    return it->second.get();
+  }
+  static R huber(R x, R a) { return std::fabs(x) < a ? (R)0.5f * (x * x) / a : std::fabs(x) - (R)0.5f * a; }
+
+  // PrimalDualInit (optimize/primal_dual.cu:15-40) with GetInitSDFGradient
+  // (geometry/primal_dual_query.h:45-87)
+  void huber_init() {
+    pd.clear();
+    for (int id : cand) pd[id].reset(new PDB());
+    for (int id : cand) {
+      Blk<R> *b = blocks[id].get();
+      PDB *s = pd[id].get();
+      for (int i = 0; i < kBV; ++i) s->mask[i] = false;
+      for (int i = 0; i < kBV; ++i) {
+        if (b->w[i] < (R)1e-6f) continue;
+        I3 v{b->x * kB + i % kB, b->y * kB + (i / kB) % kB, b->z * kB + i / (kB * kB)};
+        V3<R> g = mk((R)0, (R)0, (R)0);
+        R q[3];
+        bool ok = true;
+        for (int k = 0; k < 3 && ok; ++k) {
+          int li, nid = voxel_id(step(v, k, 1), li);
+          ok = nid >= 0 && blocks[nid]->w[li] >= (R)1e-6f;
+          if (ok) q[k] = blocks[nid]->sdf[li];
+        }
+        if (ok) g = mk(q[0] - b->sdf[i], q[1] - b->sdf[i], q[2] - b->sdf[i]);
+        s->w[i] = std::exp(length(g) / vs());
+        s->sdf0[i] = b->sdf[i];
+        s->bar[i] = 0;
+        s->p[i][0] = s->p[i][1] = s->p[i][2] = 0;
+        s->mask[i] = true;
+      }
+    }
+  }
+
+  // forward differences of the sdf (bar = false) or of sdf_bar (bar = true)
+  // over masked neighbours (GetSDFGradient / GetPrimalGradient,
+  // primal_dual_query.h:90-133 and 188-231)
+  V3<R> pd_grad(I3 v, R c, bool bar) const {
+    R q[3];
+    for (int k = 0; k < 3; ++k) {
+      int li;
+      const PDB *n = pd_usable(step(v, k, 1), li);
+      if (!n) return mk((R)0, (R)0, (R)0);
+      q[k] = bar ? n->bar[li] : blocks[voxel_id(step(v, k, 1), li)]->sdf[li];
+    }
+    return mk(q[0] - c, q[1] - c, q[2] - c);
+  }
+
+  // PrimalDualIterate (optimize/primal_dual.cu:176-223): pass 1 (dual step and
+  // energies, :44-104), then pass 2 (primal step, :106-143), iters times
+  void huber_iterate(R lambda, R sigma, R tau, int iters) {
+    const R alpha = (R)0.02f;
+    for (int it = 0; it < iters; ++it) {
+      double ed = 0, et = 0;
+      for (int id : cand) {
+        auto f = pd.find(id);
+        if (f == pd.end()) continue;
+        Blk<R> *b = blocks[id].get();
+        PDB *s = f->second.get();
+        for (int i = 0; i < kBV; ++i) {
+          if (b->w[i] < (R)1e-6f || !s->mask[i]) continue;
+          I3 v{b->x * kB + i % kB, b->y * kB + (i / kB) % kB, b->z * kB + i / (kB * kB)};
+          R dd = std::fabs(b->sdf[i] - s->sdf0[i]);
+          ed += (double)(dd * dd);
+          et += (double)huber(length(pd_grad(v, b->sdf[i], false)), alpha);
+          V3<R> g = pd_grad(v, s->bar[i], true);
+          R px = s->p[i][0] + sigma * g.x, py = s->p[i][1] + sigma * g.y, pz = s->p[i][2] + sigma * g.z;
+          R h = (R)1 + sigma * alpha;
+          px /= h, py /= h, pz /= h;
+          R nrm = std::max((R)1, std::sqrt(px * px + py * py + pz * pz));
+          s->p[i][0] = px / nrm, s->p[i][1] = py / nrm, s->p[i][2] = pz / nrm;
+        }
+      }
+      pd_err[0] = ed, pd_err[1] = et;
+      for (int id : cand) {
+        auto f = pd.find(id);
+        if (f == pd.end()) continue;
+        Blk<R> *b = blocks[id].get();
+        PDB *s = f->second.get();
+        for (int i = 0; i < kBV; ++i) {
+          if (b->w[i] < (R)1e-6f || !s->mask[i]) continue;
+          I3 v{b->x * kB + i % kB, b->y * kB + (i / kB) % kB, b->z * kB + i / (kB * kB)};
+          // GetDualDivergence (primal_dual_query.h:136-185): backward neighbours
+          R div = 0, pn[3];
+          bool ok = true;
+          for (int k = 0; k < 3 && ok; ++k) {
+            int li;
+            const PDB *n = pd_usable(step(v, k, -1), li);
+            ok = n != nullptr;
+            if (ok) pn[k] = n->p[li][k];
+          }
+          if (ok) div = (pn[0] - s->p[i][0]) + (pn[1] - s->p[i][1]) + (pn[2] - s->p[i][2]);
+          R prev = b->sdf[i];
+          R lam = lambda * s->w[i];
+          R x = prev - tau * div;
+          x = (x + lam * tau * s->sdf0[i]) / ((R)1 + lam * tau);
+          if (s->w[i] > (R)2) x = s->sdf0[i];
+          b->sdf[i] = x;
+          s->bar[i] = (R)2 * x - prev;
+        }
+      }
+    }
+  }
+
   // ---------------------------------------------------------- queries
   // GetVoxelValue by voxel coordinate (geometry/voxel_query.h:78-99)
   const Blk<R> *block_of(I3 v, int &li) const {
@@ -1831,6 +1962,18 @@ int orc_gc_recycle(void *hp) {
   int n = 0;
   DISPATCH(h, n = vol->gc_recycle());
   return n;
+}
+
+void orc_huber_init(void *hp) {
+  OHandle *h = (OHandle *)hp;
+  DISPATCH(h, vol->huber_init());
+}
+void orc_huber_iterate(void *hp, float lambda, float sigma, float tau, int iters, double *err) {
+  OHandle *h = (OHandle *)hp;
+  DISPATCH(h, {
+    vol->huber_iterate(lambda, sigma, tau, iters);
+    err[0] = vol->pd_err[0], err[1] = vol->pd_err[1];
+  });
 }
 
 void orc_denoise_tv(void *hp, float lambda, int iters) {

@@ -79,6 +79,8 @@ def lib():
         L.orc_frame.argtypes = [vp, f32p, f32p, C.c_int, C.c_float, f32p, f32p, f32p]
         L.orc_denoise_tv.argtypes = [vp, C.c_float, C.c_int]
         L.orc_get_depth.argtypes = [vp, f32p]
+        L.orc_huber_init.argtypes = [vp]
+        L.orc_huber_iterate.argtypes = [vp, C.c_float, C.c_float, C.c_float, C.c_int, C.POINTER(C.c_double)]
         L.orc_debug_ray.argtypes = [vp, f32p, C.c_int, C.c_int, C.POINTER(C.c_double)]
         L.orc_raycast_backward.argtypes = [vp, f32p, f32p, f32p, C.POINTER(C.c_double)]
         L.orc_grad_blocks.restype = C.c_int
@@ -260,6 +262,17 @@ class Oracle:
 
     def denoise_tv(self, lam=0.1, iterations=20):
         self.L.orc_denoise_tv(self.h, float(lam), int(iterations))
+
+    def huber_tv_init(self):
+        """PrimalDualInit over the current candidate blocks."""
+        self.L.orc_huber_init(self.h)
+
+    def huber_tv_iterate(self, lam, sigma, tau, iterations=1):
+        """Dual + primal steps; returns [lam/2 data + tv, data, tv] of the
+        last iteration's dual pass."""
+        e = (C.c_double * 2)()
+        self.L.orc_huber_iterate(self.h, float(lam), float(sigma), float(tau), int(iterations), e)
+        return np.array([e[0] * np.float32(lam) / 2 + e[1], e[0], e[1]])
 
     def depth(self):
         out = np.zeros(self.W * self.H, np.float32)
