@@ -281,8 +281,9 @@ int mh_load_volume(mh_volume *v, const char *path, int *n_blocks);
 /* Volumetric Huber-TV smoothing of the sdf over the current candidate blocks
  * (PrimalDualInit / PrimalDualIterate, optimize/primal_dual.cu:10-223; the
  * reference never calls them).  init records sdf0 and the per-voxel data
- * weight exp(|grad sdf| / voxel) and allocates the state on first use (28 B
- * per voxel of the block pool); iterate runs dual + primal steps and writes
+ * weight exp(|grad sdf| / voxel) and allocates the state on first use (32 B
+ * per voxel of the block pool; pools up to 2^23 blocks, else MH_ERR_INVALID);
+ * iterate runs dual + primal steps and writes
  * the smoothed sdf in place.  energy (may be NULL): [lambda/2 data + tv, data,
  * tv] before the last iteration's primal step, as the reference reports it. */
 int mh_huber_tv_init(mh_volume *v, void *stream);

@@ -6,7 +6,7 @@ the reference tree, so it runs only where that tree is present (this is how
 tests/golden/ fixtures are produced; see tests/golden/make_golden.py).
 ``RefCPU`` drives the reference's stages (AllocBlockArray,
 CollectBlocksInFrustum, UpdateBlocksSimple / Bayesian, MarchingCubes, GC,
-RayCaster::Cast) with the reference's launch shapes, one emulated CUDA
+RayCaster::Cast, PrimalDualInit / Iterate) with the reference's launch shapes, one emulated CUDA
 thread at a time.
 """
 from __future__ import annotations
@@ -71,6 +71,10 @@ def lib():
         L.ref_dump_mesh.argtypes = [vp, C.c_int, i32p, f32p, C.c_int, i32p, i32p, i32p]
         L.ref_inverse.argtypes = [f32p, f32p]
         L.ref_cube_indices.argtypes = [vp, C.c_int, i32p, C.POINTER(C.c_uint8)]
+        L.ref_pd_init.argtypes = [vp]
+        L.ref_set_candidates.restype = C.c_int
+        L.ref_set_candidates.argtypes = [vp, C.c_int, i32p]
+        L.ref_pd_iterate.argtypes = [vp, C.c_float, C.c_float, C.c_float, f32p]
         _lib = L
     return _lib
 
@@ -126,6 +130,19 @@ class RefCPU:
 
     def gc_recycle(self):
         self.L.ref_gc_recycle(self.h)
+
+    def set_candidates(self, pos):
+        pos = np.ascontiguousarray(pos, np.int32).reshape(-1, 3)
+        return self.L.ref_set_candidates(self.h, len(pos), _p(pos, C.c_int32))
+
+    def pd_init(self):
+        self.L.ref_pd_init(self.h)
+
+    def pd_iterate(self, lam, sigma, tau):
+        """One PrimalDualIterate; returns (err_data, err_tv) of its pass 1."""
+        e = np.zeros(2, np.float32)
+        self.L.ref_pd_iterate(self.h, float(lam), float(sigma), float(tau), _p(e, C.c_float))
+        return e
 
     def raycast(self, cTw):
         W, H = self.p.rc_width, self.p.rc_height

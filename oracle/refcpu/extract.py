@@ -23,6 +23,7 @@ SOURCES = [
     ("src/meshing/marching_cubes.cu", ()),
     ("src/visualization/ray_caster.cu", ()),
     ("src/mapping/recycle.cu", ()),
+    ("src/optimize/primal_dual.cu", ()),
 ]
 
 

@@ -11,7 +11,7 @@
 // (mapping/allocate.cu:101-125, core/collect_block_array.cu:245-276,
 // mapping/update_simple.cu:79-108, mapping/update_bayesian.cu:372-433,
 // meshing/marching_cubes.cu:326-382, mapping/recycle.cu:183-274,
-// visualization/ray_caster.cu:190-209).  Every emulated CUDA thread runs
+// visualization/ray_caster.cu:190-209, optimize/primal_dual.cu:146-223).  Every emulated CUDA thread runs
 // to completion (or to its next __syncthreads) before the next one starts.
 #include "cuda_host.h"
 #include "helper_math.h"
@@ -30,6 +30,7 @@
 #include "geometry/voxel_query.h"
 #include "geometry/spatial_query.h"
 #include "geometry/isosurface_intersection.h"
+#include "geometry/primal_dual_query.h"
 #include "visualization/color_util.h"
 #include "meshing/mc_tables.h"
 
@@ -482,6 +483,41 @@ void ref_raycast(void *h, const float *cTw, float *depth, float *normal4) {
       normal4[4 * i + 2] = nn[i].z, normal4[4 * i + 3] = nn[i].w;
     }
   }
+}
+
+// Replace the candidate list by the entries of the given block positions
+// (absent positions are skipped); returns the new count.
+int ref_set_candidates(void *h, int n, const int32_t *pos) {
+  Ref *r = (Ref *)h;
+  r->cand.reset_count();
+  for (int i = 0; i < n; ++i) {
+    HashEntry e = r->ht.GetEntry(make_int3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]));
+    if (e.ptr == FREE_ENTRY) continue;
+    r->cand[r->cand.counter()++] = e;
+  }
+  return (int)r->cand.count();
+}
+
+// PrimalDualInit / PrimalDualIterate (optimize/primal_dual.cu:146-223) with
+// the reference's launch shapes; the two error accumulators live in host
+// memory instead of cudaMalloc'd floats, and are returned instead of printed.
+void ref_pd_init(void *h) {
+  Ref *r = (Ref *)h;
+  uint n = r->cand.count();
+  if (n == 0) return;
+  launch(D3(n), D3(BLOCK_SIZE), false, [&] { PrimalDualInitKernel(r->cand, r->blocks, r->ht, r->gh); });
+}
+
+void ref_pd_iterate(void *h, float lambda, float sigma, float tau, float *err) {
+  Ref *r = (Ref *)h;
+  uint n = r->cand.count();
+  err[0] = err[1] = 0.0f;
+  if (n == 0) return;
+  launch(D3(n), D3(BLOCK_SIZE), false, [&] {
+    PrimalDualIteratePass1Kernel(r->cand, r->blocks, r->ht, r->gh, lambda, sigma, tau, err, err + 1);
+  });
+  launch(D3(n), D3(BLOCK_SIZE), false,
+         [&] { PrimalDualIteratePass2Kernel(r->cand, r->blocks, r->ht, r->gh, lambda, sigma, tau); });
 }
 
 // Live blocks: pos[3n] and voxel fields [512n] in hash-entry order.

@@ -181,3 +181,21 @@ def check_psdf(runner_cls):
     got = r.inlier()
     assert np.abs(got - fx["inlier"]).max() < 1e-5
     return worst
+
+
+def check_huber(impl):
+    """PrimalDualInit + iterations on the fixture's cluster.  impl(params,
+    pos, sdf, w, cand) returns an object with iterate(lam, sigma, tau) ->
+    [total, data, tv] and sdf(cand) -> rows.  Energies are checked here
+    against the reference's float sums; returns (final sdf, the reference's
+    final sdf, the cluster's sdf before) for the caller's precision checks."""
+    fx = load("huber_room96.npz")
+    lam, sigma, tau, iters = (float(x) for x in fx["hparams"])
+    h = impl(simple_params(), fx["pre_pos"], fx["pre_sdf"], fx["pre_w"], fx["cand"])
+    for k in range(int(iters)):
+        e = h.iterate(lam, sigma, tau)
+        # the reference adds single-precision values one by one
+        np.testing.assert_allclose(e[1:], fx["errs"][k], rtol=1e-4, atol=1e-12)
+    before = rows(fx["pre_pos"], fx["pre_sdf"], fx["cand"])
+    assert np.count_nonzero(fx["post_sdf"] != before) > 5000
+    return h.sdf(fx["cand"]), fx["post_sdf"], before

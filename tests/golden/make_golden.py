@@ -14,6 +14,11 @@ committed, so tests never need the tree.
   psdf_room96.npz    PSDF chain, 96x72, 4 mm voxels, 6 frames of the spline
                      trajectory (with outliers and missing pixels): block
                      set, voxel values of sampled blocks, inlier ratios
+  huber_room96.npz   PrimalDualInit + 8 PrimalDualIterate calls
+                     (optimize/primal_dual.cu) on a 48-block cluster of the
+                     simple chain's last candidates: the cluster's and its
+                     face neighbours' sdf and weight before, the cluster's
+                     sdf after, the two error sums of every iteration
 
 Both use params.compat_arithmetic = 1 (the reference's single-precision
 formulas as written).  Allocation is repeated until no block is added, which
@@ -105,6 +110,50 @@ def run_psdf(ref_mod, p, depth, poses):
                 sample_sdf=s[idx], sample_w=w[idx], sample_a=a[idx], sample_b=b[idx], inlier=r.inlier())
 
 
+HUBER = dict(lam=2.0, sigma=8.0, tau=0.01, iterations=8, blocks=48)
+FACES = [(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)]
+
+
+def huber_cluster(cand, pos, w, n):
+    """The n candidates nearest (Chebyshev distance, then position) to the
+    candidate with the most observed voxels."""
+    idx = {tuple(q): i for i, q in enumerate(pos.tolist())}
+    obs = np.array([(w[idx[tuple(q)]] > 0).sum() for q in cand.tolist()])
+    c0 = cand[int(np.argmax(obs))]
+    d = np.abs(cand - c0).max(axis=1)
+    order = np.lexsort((cand[:, 2], cand[:, 1], cand[:, 0], d))
+    return cand[order[:n]]
+
+
+def run_huber(ref_mod, p, depth, poses):
+    r = ref_mod.RefCPU(p)
+    for d, T in zip(depth, poses):
+        r.frame_set(d, T)
+        r.alloc(True)
+        r.collect()
+        r.integrate_simple()
+        r.mesh()
+        r.gc_low_surfel()
+    pos, s, w, _, _ = r.blocks()
+    cl = huber_cluster(r.candidates(), pos, w, HUBER["blocks"])
+    have = {tuple(q) for q in pos.tolist()}
+    near = {tuple(q) for q in cl.tolist()}
+    near |= {(q[0] + f[0], q[1] + f[1], q[2] + f[2]) for q in cl.tolist() for f in FACES}
+    near = np.array(sorted(q for q in near if q in have), np.int32)
+    assert r.set_candidates(cl) == len(cl)
+    r.pd_init()
+    errs = np.stack([r.pd_iterate(HUBER["lam"], HUBER["sigma"], HUBER["tau"]) for _ in range(HUBER["iterations"])])
+    pos2, s2, _, _, _ = r.blocks()
+    return dict(pre_pos=near, pre_sdf=rows(pos, s, near), pre_w=rows(pos, w, near), cand=cl,
+                post_sdf=rows(pos2, s2, cl), errs=errs,
+                hparams=np.array([HUBER["lam"], HUBER["sigma"], HUBER["tau"], HUBER["iterations"]], np.float32))
+
+
+def rows(pos, field, want):
+    idx = {tuple(q): i for i, q in enumerate(pos.tolist())}
+    return np.stack([field[idx[tuple(q)]] for q in np.asarray(want).tolist()])
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     from oracle import refcpu
@@ -113,7 +162,9 @@ def main():
     np.savez_compressed(os.path.join(HERE, "simple_room96.npz"), **run_simple(refcpu, p, depth, poses))
     p, depth, poses = psdf_case()
     np.savez_compressed(os.path.join(HERE, "psdf_room96.npz"), **run_psdf(refcpu, p, depth, poses))
-    for f in ("simple_room96.npz", "psdf_room96.npz"):
+    p, depth, poses = simple_case()
+    np.savez_compressed(os.path.join(HERE, "huber_room96.npz"), **run_huber(refcpu, p, depth, poses))
+    for f in ("simple_room96.npz", "psdf_room96.npz", "huber_room96.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

@@ -4,7 +4,8 @@ tests/golden/*.npz hold seeded inputs and the outputs of the reference's
 kernels built for the CPU (see tests/golden/make_golden.py).  With
 compat_arithmetic = 1 the oracle must reproduce them bit for bit (voxel
 values, block sets, mesh topology, raycast depth); PSDF values within a few
-ulp (expf).  The GPU counterpart is tests/test_gpu_golden.py.
+ulp (expf); the volumetric Huber-TV (optimize/primal_dual.cu) bit for bit.
+The GPU counterpart is tests/test_gpu_golden.py.
 """
 import os
 
@@ -22,6 +23,30 @@ def test_oracle_matches_reference_psdf_chain(built):
     _golden.check_psdf(_golden.OracleRunner)
 
 
+class _OracleHuber:
+    def __init__(self, params, pos, sdf, w, cand):
+        import numpy as np
+        from oracle.oracle import Oracle
+        self.o = Oracle(params, fp64=False)
+        z = np.zeros_like(sdf)
+        self.o.set_blocks(pos, sdf, w, z, z)
+        self.o.set_candidates(cand)
+        self.o.huber_tv_init()
+
+    def iterate(self, lam, sigma, tau):
+        return self.o.huber_tv_iterate(lam, sigma, tau, 1)
+
+    def sdf(self, cand):
+        pos, s = self.o.blocks()[:2]
+        return _golden.rows(pos, s, cand)
+
+
+def test_oracle_matches_reference_huber_tv(built):
+    import numpy as np
+    got, want, _ = _golden.check_huber(_OracleHuber)
+    np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
 @pytest.mark.skipif(not os.path.isdir("/root/reference"), reason="reference sources not present")
 def test_fixtures_regenerate_from_reference(built, tmp_path):
     """The committed fixtures are what the reference's code produces now."""
@@ -37,4 +62,8 @@ def test_fixtures_regenerate_from_reference(built, tmp_path):
     np.testing.assert_array_equal(depth, fx["depth"])
     out = mg.run_simple(refcpu, p, depth, poses)
     for k in ("counts", "blocks", "sample_sdf", "sample_w", "tris", "ray_depth"):
+        np.testing.assert_array_equal(out[k], fx[k])
+    out = mg.run_huber(refcpu, p, depth, poses)
+    fx = _golden.load("huber_room96.npz")
+    for k in ("pre_pos", "pre_sdf", "pre_w", "cand", "post_sdf", "errs"):
         np.testing.assert_array_equal(out[k], fx[k])
