@@ -203,6 +203,7 @@ def run_pose_refinement(vol, frames, poses, W, H, iterations=10):
     from meshhashing_gb300.pose import left_update, pose_error
     rng = np.random.default_rng(77)
     start, final, ms = [], [], []
+    p2p = {"reference": ([], []), "fixed_jacobian": ([], [])}
     for d, T in zip(frames, poses):
         T_true = np.asarray(T, np.float64)
         xi = np.concatenate([rng.standard_normal(3) * 0.02, rng.standard_normal(3) * np.radians(1.0)])
@@ -214,6 +215,15 @@ def run_pose_refinement(vol, frames, poses, W, H, iterations=10):
         ms.append((time.perf_counter() - t0) * 1000.0)
         start.append(pose_error(T0, T_true))
         final.append(pose_error(T_ref, T_true))
+        # the reference's point-to-PSDF tracker from the same start: its own
+        # damping and Jacobian, then Gauss-Newton with the corrected Jacobian
+        for key, lam, ref_j in (("reference", 1e5, True), ("fixed_jacobian", 1.0, False)):
+            vol.set_frame(d, T0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            T_p, _, _ = vol.track_point_to_psdf(T0, iterations=iterations, lam=lam, reference_jacobian=ref_j)
+            p2p[key][0].append((time.perf_counter() - t0) * 1000.0)
+            p2p[key][1].append(pose_error(T_p, T_true))
     cTw = np.linalg.inv(np.asarray(poses[0], np.float64)).astype(np.float32)
     dl = torch.randn((H, W), generator=torch.Generator().manual_seed(3)).cuda()
     grad = torch.zeros(vol.params.value_capacity * 512, dtype=torch.float32, device="cuda")
@@ -228,7 +238,12 @@ def run_pose_refinement(vol, frames, poses, W, H, iterations=10):
             "final_error": {"mm": med(final, 0) * 1000.0, "deg": med(final, 1)},
             "final_error_max": {"mm": max(x[0] for x in final) * 1000.0, "deg": max(x[1] for x in final)},
             "raycast_backward_ms": bw_ms,
-            "note": "median over frames; perturbation sigma 1 deg / 2 cm per axis; PSDF map of this run"}
+            "point_to_psdf": {k: {"ms_per_frame": float(np.median(v[0])), "final_error": {"mm": med(v[1], 0) * 1000.0,
+                                                                                          "deg": med(v[1], 1)}}
+                              for k, v in p2p.items()},
+            "note": "median over frames; perturbation sigma 1 deg / 2 cm per axis; PSDF map of this run; "
+                    "point_to_psdf: the reference's tracker (MainEngine::Localizing) from the same starts, "
+                    "with its lambda 1e5 and J[2] = dD/dx, and with lambda 1 and the corrected Jacobian"}
 
 
 def run_huber_tv(vol, peak, iterations=10):

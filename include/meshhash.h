@@ -267,6 +267,9 @@ int mh_mesh_compact(mh_volume *v, int max_vertices, float *positions3, float *no
 /* The dense mesh as a binary little-endian PLY file (io/mesh_writer.cc:14-150
  * writes the reference's): float x y z nx ny nz per vertex, uchar-int lists. */
 int mh_write_ply(mh_volume *v, const char *path);
+/* The same mesh as Wavefront OBJ text (SaveObj, io/mesh_writer.cc:14-73):
+ * v, vn and 1-based "f a//a b//b c//c" lines. */
+int mh_write_obj(mh_volume *v, const char *path);
 
 /* Block checkpoint (the reference's block recording,
  * engine/logging_engine.cc:101-233): every allocated block's position and
@@ -326,6 +329,23 @@ int mh_raycast_normal_equations(mh_volume *v, const float cTw[16], const float *
  * NULL): the residual at the returned pose. */
 int mh_refine_pose(mh_volume *v, const float *obs_depth, float wTc[16], int iterations, float max_residual,
                    double *final_cost, int *final_count, void *stream);
+
+/* The reference's tracker, MainEngine::Localizing (engine/main_engine.cc:70-98)
+ * over PointToSurface (localizing/point_to_psdf.cu:19-147).  Normal
+ * equations of the point-to-PSDF residual at pose wTc over the current
+ * frame's pixels with odd x and y: A = sum J J^T (6 x 6 row-major),
+ * b = sum D J, err = sum D^2, count; D is the trilinear sdf at the
+ * frame point moved to the world, J = [grad D, p x grad D].  The reference
+ * writes J[2] = dD/dx (point_to_psdf.cu:70); reference_jacobian = 1 keeps
+ * that, 0 uses dD/dz.  Needs a frame (mh_frame_set). */
+int mh_point_to_psdf_normal_equations(mh_volume *v, const float wTc[16], int reference_jacobian, double A[36],
+                                      double b[6], double *err, int *count, void *stream);
+/* `iterations` steps dxi = -(A + lambda I)^-1 b, wTc <- exp(dxi) wTc (the
+ * reference uses lambda = 1e5), stopping when no pixel contributes; wTc is
+ * updated in place and becomes the frame's pose.  final_err / final_count
+ * (may be NULL): the sums of the last evaluated pose. */
+int mh_track_point_to_psdf(mh_volume *v, float wTc[16], int iterations, float lambda, int reference_jacobian,
+                           double *final_err, int *final_count, void *stream);
 /* Like mh_dump_blocks for a caller's device field laid out like the voxel
  * storage (value_capacity x 512 floats), e.g. the grad_sdf above. */
 int mh_dump_block_field(mh_volume *v, const float *field, int max_blocks, int32_t *pos, float *out, int *n_out);

@@ -66,8 +66,12 @@ SIGNATURES = {
                                           C.POINTER(C.c_double), C.POINTER(C.c_int32), vp]),
     "mh_refine_pose": (i32, [MHV, vp, f32p, i32, C.c_float, C.POINTER(C.c_double), C.POINTER(C.c_int32), vp]),
     "mh_dump_block_field": (i32, [MHV, vp, i32, i32p, f32p, i32p]),
+    "mh_point_to_psdf_normal_equations": (i32, [MHV, f32p, i32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                                C.POINTER(C.c_double), i32p, vp]),
+    "mh_track_point_to_psdf": (i32, [MHV, f32p, i32, C.c_float, i32, C.POINTER(C.c_double), i32p, vp]),
     "mh_mesh_compact": (i32, [MHV, i32, vp, vp, i32, vp, i32p, i32p, i32, vp]),
     "mh_write_ply": (i32, [MHV, C.c_char_p]),
+    "mh_write_obj": (i32, [MHV, C.c_char_p]),
     "mh_save_volume": (i32, [MHV, C.c_char_p]),
     "mh_load_volume": (i32, [MHV, C.c_char_p, i32p]),
     "mh_huber_tv_init": (i32, [MHV, vp]),

@@ -217,14 +217,21 @@ int mh_mesh_compact(mh_volume *v, int max_vertices, float *positions3, float *no
   return r;
 }
 
-int mh_write_ply(mh_volume *v, const char *path) {
-  if (!v || !path) return MH_ERR_INVALID;
-  int nv = 0, nt = 0;
+static int fetch_compact(mh_volume *v, std::vector<float> &pos, std::vector<float> &nrm, std::vector<int32_t> &tri,
+                         int &nv, int &nt) {
+  nv = nt = 0;
   int r = mh_mesh_compact(v, 0, nullptr, nullptr, 0, nullptr, &nv, &nt, 0, nullptr);
   if (r != MH_OK) return r;
-  std::vector<float> pos((size_t)nv * 3), nrm((size_t)nv * 3);
-  std::vector<int32_t> tri((size_t)nt * 3);
-  r = mh_mesh_compact(v, nv, pos.data(), nrm.data(), nt, tri.data(), &nv, &nt, 0, nullptr);
+  pos.resize((size_t)nv * 3), nrm.resize((size_t)nv * 3), tri.resize((size_t)nt * 3);
+  return mh_mesh_compact(v, nv, pos.data(), nrm.data(), nt, tri.data(), &nv, &nt, 0, nullptr);
+}
+
+int mh_write_ply(mh_volume *v, const char *path) {
+  if (!v || !path) return MH_ERR_INVALID;
+  std::vector<float> pos, nrm;
+  std::vector<int32_t> tri;
+  int nv, nt;
+  int r = fetch_compact(v, pos, nrm, tri, nv, nt);
   if (r != MH_OK) return r;
   FILE *f = fopen(path, "wb");
   if (!f) return MH_ERR_INVALID;
@@ -241,6 +248,31 @@ int mh_write_ply(mh_volume *v, const char *path) {
   for (int i = 0; i < nt && ok; ++i) {
     const unsigned char three = 3;
     ok = fwrite(&three, 1, 1, f) == 1 && fwrite(&tri[3 * i], sizeof(int32_t), 3, f) == 3;
+  }
+  ok = (fclose(f) == 0) && ok;
+  return ok ? MH_OK : MH_ERR_INVALID;
+}
+
+// SaveObj (io/mesh_writer.cc:14-73): "v", then "vn" lines, then faces as
+// 1-based "f a//a b//b c//c"; coordinates with 9 significant digits, which
+// read back to the same floats.
+int mh_write_obj(mh_volume *v, const char *path) {
+  if (!v || !path) return MH_ERR_INVALID;
+  std::vector<float> pos, nrm;
+  std::vector<int32_t> tri;
+  int nv, nt;
+  int r = fetch_compact(v, pos, nrm, tri, nv, nt);
+  if (r != MH_OK) return r;
+  FILE *f = fopen(path, "w");
+  if (!f) return MH_ERR_INVALID;
+  bool ok = true;
+  for (int i = 0; i < nv && ok; ++i)
+    ok = fprintf(f, "v %.9g %.9g %.9g\n", pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]) > 0;
+  for (int i = 0; i < nv && ok; ++i)
+    ok = fprintf(f, "vn %.9g %.9g %.9g\n", nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]) > 0;
+  for (int i = 0; i < nt && ok; ++i) {
+    const int a = tri[3 * i] + 1, b = tri[3 * i + 1] + 1, c = tri[3 * i + 2] + 1;
+    ok = fprintf(f, "f %d//%d %d//%d %d//%d\n", a, a, b, b, c, c) > 0;
   }
   ok = (fclose(f) == 0) && ok;
   return ok ? MH_OK : MH_ERR_INVALID;

@@ -2,12 +2,13 @@
 // rendered depth and normals, Gauss-Newton normal equations of depth
 // alignment, and frame-to-model pose refinement driven by them.
 //
-// No reference counterpart for the gradients; the reference tracks with a
-// point-to-PSDF Gauss-Newton over surface points (localizing/point_to_psdf.cu),
-// while here the residual is the rendered depth against the observed depth
-// of the same pixel, differentiated through the raycast itself (kernels in
-// mh_raycast.cu).  Pose perturbations are left se(3) increments
-// wTc <- exp(xi) wTc with xi = (v, w): translation first, then rotation.
+// No reference counterpart for the gradients.  Two trackers: the reference's
+// point-to-PSDF Gauss-Newton over the frame's points (localizing/
+// point_to_psdf.cu, MainEngine::Localizing), and a projective point-to-plane
+// refinement against the raycast of the model, differentiated through the
+// raycast itself (kernels in mh_raycast.cu).  Pose perturbations are left
+// se(3) increments wTc <- exp(xi) wTc with xi = (v, w): translation first,
+// then rotation (Sophus's tangent order).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -105,9 +106,141 @@ bool solve6(const double A_in[36], const double b[6], double x[6]) {
   return true;
 }
 
+// the pose becomes the frame's pose for the mapping stages and the raycast
+int adopt_frame_pose(mh_volume *v, const float wTc[16], cudaStream_t s) {
+  if (!v->has_frame) return MH_OK;
+  FrameConst &fc = v->fc_host;
+  memcpy(fc.wTc, wTc, sizeof(float) * 16);
+  inverse4(fc.wTc, fc.cTw);
+  memcpy(fc.rc_cTw, fc.cTw, sizeof(float) * 16);
+  inverse4(fc.rc_cTw, fc.rc_wTc);
+  return cudaMemcpyAsync(v->d.fc, &fc, sizeof(FrameConst), cudaMemcpyHostToDevice, s) == cudaSuccess ? MH_OK
+                                                                                                      : MH_ERR_CUDA;
+}
+
+struct Pose16 {
+  float m[16];
+};
+
+// PointToSurfaceKernel (localizing/point_to_psdf.cu:19-84): one thread per
+// pixel with odd x and odd y.  A valid depth is reprojected
+// (ImageReprojectToCamera, geometry_helper.h:164-170), moved to the world by
+// wTc, and contributes when its trilinear sdf D and gradient g both exist:
+// J = [g, p x g] (the reference writes J[2] = g.x, point_to_psdf.cu:70,
+// kept when ref_j is set), A += J J^T, b += D J, err += D^2, count += 1.
+// acc = [A upper triangle (21), b (6), err, count], CTA sums added as doubles.
+__global__ void __launch_bounds__(256) k_point_to_psdf(Dev d, Pose16 T, int ref_j, double *acc) {
+  const DevParams &p = d.p;
+  const unsigned x = 2 * (blockIdx.x * 16 + threadIdx.x) + 1, y = 2 * (blockIdx.y * 16 + threadIdx.y) + 1;
+  float v[29];
+#pragma unroll
+  for (int k = 0; k < 29; ++k) v[k] = 0.0f;
+  if (x < p.width && y < p.height) {
+    const float dep = d.depth[(size_t)y * p.width + x];
+    if (!depth_invalid(p, dep)) {
+      const float rx = ((float)x - p.cx) / p.fx, ry = ((float)y - p.cy) / p.fy;
+      const F3 pw = mul_pt(T.m, f3(dep * rx, dep * ry, dep));
+      BlockCache bc, bc2;
+      bc.init();
+      bc2.init();
+      float s, r;
+      F3 g;
+      if (spatial_sample<false>(d, bc, pw, s, r, &bc2) && spatial_gradient(d, bc, pw, g)) {
+        const float J[6] = {g.x, g.y, ref_j ? g.x : g.z, -g.y * pw.z + g.z * pw.y, -g.z * pw.x + g.x * pw.z,
+                            -g.x * pw.y + g.y * pw.x};
+        int k = 0;
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+          for (int j = i; j < 6; ++j) v[k++] = J[i] * J[j];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) v[21 + i] = s * J[i];
+        v[27] = s * s;
+        v[28] = 1.0f;
+      }
+    }
+  }
+  __shared__ float red[29][8];
+  const int tid = threadIdx.x + 16 * threadIdx.y, lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+  for (int k = 0; k < 29; ++k) {
+    float z = v[k];
+    for (int o = 16; o; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
+    if (lane == 0) red[k][wid] = z;
+  }
+  __syncthreads();
+  if (tid < 29) {
+    double sum = 0.0;
+    for (int w = 0; w < 8; ++w) sum += red[tid][w];
+    if (sum != 0.0) atomicAdd(acc + tid, sum);
+  }
+}
+
 }  // namespace
 
 extern "C" {
+
+int mh_point_to_psdf_normal_equations(mh_volume *v, const float wTc[16], int reference_jacobian, double A[36],
+                                      double b[6], double *err, int *count, void *stream) {
+  if (!v || !wTc) return MH_ERR_INVALID;
+  if (!v->has_frame) return MH_ERR_STATE;
+  cudaStream_t s = (cudaStream_t)stream;
+  int r;
+  if ((r = ensure_acc(v)) != MH_OK) return r;
+  if (cudaMemsetAsync(v->acc, 0, sizeof(double) * 32, s) != cudaSuccess) return MH_ERR_CUDA;
+  Pose16 T;
+  memcpy(T.m, wTc, sizeof(T.m));
+  const unsigned hw = (v->hp.width / 2 + 15) / 16, hh = (v->hp.height / 2 + 15) / 16;
+  k_point_to_psdf<<<dim3(hw ? hw : 1, hh ? hh : 1), dim3(16, 16), 0, s>>>(v->d, T, reference_jacobian ? 1 : 0,
+                                                                          v->acc);
+  mh_count_launches(1);
+  if (cudaGetLastError() != cudaSuccess) return MH_ERR_CUDA;
+  double h[29];
+  if (cudaMemcpyAsync(h, v->acc, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return MH_ERR_CUDA;
+  if (A) {
+    int k = 0;
+    for (int i = 0; i < 6; ++i)
+      for (int j = i; j < 6; ++j, ++k) A[6 * i + j] = A[6 * j + i] = h[k];
+  }
+  if (b) memcpy(b, h + 21, sizeof(double) * 6);
+  if (err) *err = h[27];
+  if (count) *count = (int)h[28];
+  return MH_OK;
+}
+
+// MainEngine::Localizing (engine/main_engine.cc:70-98): per iteration the
+// normal equations at the current pose; none -> stop; otherwise
+// dxi = -(A + lambda I)^-1 b and wTc <- exp(dxi) wTc (SolveAndConvertDeltaXi,
+// main_engine.cc:28-54, with Eigen's LDLT and Sophus's exp restated: a
+// Cholesky solve and the closed-form SE(3) exponential, in double).
+int mh_track_point_to_psdf(mh_volume *v, float wTc[16], int iterations, float lambda, int reference_jacobian,
+                           double *final_err, int *final_count, void *stream) {
+  if (!v || !wTc || iterations < 0 || !(lambda >= 0.0f)) return MH_ERR_INVALID;
+  if (!v->has_frame) return MH_ERR_STATE;
+  double T[16];
+  for (int i = 0; i < 16; ++i) T[i] = wTc[i];
+  double err = 0.0;
+  int count = 0;
+  for (int it = 0; it < iterations; ++it) {
+    float Tf[16];
+    for (int i = 0; i < 16; ++i) Tf[i] = (float)T[i];
+    double A[36], b[6];
+    int r = mh_point_to_psdf_normal_equations(v, Tf, reference_jacobian, A, b, &err, &count, stream);
+    if (r != MH_OK) return r;
+    if (count == 0) break;
+    for (int i = 0; i < 6; ++i) A[7 * i] += lambda;
+    double nb[6], x[6];
+    for (int i = 0; i < 6; ++i) nb[i] = -b[i];
+    if (!solve6(A, nb, x)) break;
+    se3_left_update(x, T);
+  }
+  for (int i = 0; i < 16; ++i) wTc[i] = (float)T[i];
+  if (final_err) *final_err = err;
+  if (final_count) *final_count = count;
+  return adopt_frame_pose(v, wTc, (cudaStream_t)stream);
+}
 
 int mh_raycast_backward(mh_volume *v, const float cTw[16], const float *dL_ddepth, const float *dL_dnormal4,
                         float *grad_sdf, double dL_dxi[6], void *stream) {
@@ -189,17 +322,7 @@ int mh_refine_pose(mh_volume *v, const float *obs_depth, float wTc[16], int iter
   if (final_cost) *final_cost = cost;
   if (final_count) *final_count = count;
   // the refined pose becomes the frame's pose for the mapping stages
-  if (v->has_frame) {
-    FrameConst &fc = v->fc_host;
-    memcpy(fc.wTc, wTc, sizeof(float) * 16);
-    inverse4(fc.wTc, fc.cTw);
-    memcpy(fc.rc_cTw, fc.cTw, sizeof(float) * 16);
-    inverse4(fc.rc_cTw, fc.rc_wTc);
-    if (cudaMemcpyAsync(v->d.fc, &fc, sizeof(FrameConst), cudaMemcpyHostToDevice, (cudaStream_t)stream) !=
-        cudaSuccess)
-      return MH_ERR_CUDA;
-  }
-  return MH_OK;
+  return adopt_frame_pose(v, wTc, (cudaStream_t)stream);
 }
 
 int mh_dump_block_field(mh_volume *v, const float *field, int max_blocks, int32_t *pos, float *out, int *n_out) {

@@ -183,6 +183,9 @@ class Volume:
     def write_ply(self, path: str):
         self._c("mh_write_ply", str(path).encode())
 
+    def write_obj(self, path: str):
+        self._c("mh_write_obj", str(path).encode())
+
     def save(self, path: str):
         """Block checkpoint (positions and voxel fields) to a file."""
         self._c("mh_save_volume", str(path).encode())
@@ -239,6 +242,25 @@ class Volume:
         self._c("mh_refine_pose", _dev(obs_depth), _ptr(m), int(iterations), C.c_float(max_residual), C.byref(cost),
                 C.byref(cnt), self.stream)
         return m.reshape(4, 4), cost.value, cnt.value
+
+    def point_to_psdf(self, wTc, reference_jacobian: bool = False):
+        """Normal equations of the reference's point-to-PSDF tracker at wTc
+        over the current frame: (A[6, 6], b[6], err, count)."""
+        m = _f32(wTc).reshape(16)
+        A, b, e, n = (C.c_double * 36)(), (C.c_double * 6)(), C.c_double(), C.c_int32()
+        self._c("mh_point_to_psdf_normal_equations", _ptr(m), 1 if reference_jacobian else 0, A, b, C.byref(e),
+                C.byref(n), self.stream)
+        return np.array(list(A)).reshape(6, 6), np.array(list(b)), e.value, n.value
+
+    def track_point_to_psdf(self, wTc, iterations: int = 10, lam: float = 1e5, reference_jacobian: bool = False):
+        """The reference's tracker (MainEngine::Localizing): returns the
+        tracked pose, the last sum of squared sdf and its point count; the
+        pose becomes the frame's."""
+        m = _f32(wTc).reshape(16).copy()
+        e, n = C.c_double(), C.c_int32()
+        self._c("mh_track_point_to_psdf", _ptr(m), int(iterations), C.c_float(lam), 1 if reference_jacobian else 0,
+                C.byref(e), C.byref(n), self.stream)
+        return m.reshape(4, 4).astype(np.float64), e.value, n.value
 
     def dump_block_field(self, field):
         """(positions, rows) of a device per-voxel field laid out like the

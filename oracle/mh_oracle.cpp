@@ -884,6 +884,38 @@ template <class R> struct Vol {
     return true;
   }
 
+  // ---------------------------------------------------------- tracking
+  // PointToSurfaceKernel (localizing/point_to_psdf.cu:19-84): over the odd
+  // pixels (x and y odd) with a valid depth, the frame point moved to the
+  // world by T, its trilinear sdf D and gradient g (both must exist), and
+  // J = [g, p x g]; sums of J J^T, D J, D^2 and the count, in double.  The
+  // reference writes J[2] = g.x (point_to_psdf.cu:70); fix_j uses g.z.
+  void point_to_psdf(const M4<R> &T, bool fix_j, double *A, double *b, double &err, int &count) const {
+    for (int i = 0; i < 36; ++i) A[i] = 0.0;
+    for (int i = 0; i < 6; ++i) b[i] = 0.0;
+    err = 0.0;
+    count = 0;
+    for (unsigned y = 1; y < p.height; y += 2) {
+      for (unsigned x = 1; x < p.width; x += 2) {
+        float df = depth[(size_t)y * p.width + x];
+        if (depth_invalid(df)) continue;
+        V3<R> pc = reproject(x, y, (R)df, (R)p.fx, (R)p.fy, (R)p.cx, (R)p.cy);
+        V3<R> pw = T.pt(pc);
+        R d;
+        V3<R> g;
+        if (!spatial(pw, d) || !gradient(pw, g)) continue;
+        R J[6] = {g.x, g.y, fix_j ? g.z : g.x, -g.y * pw.z + g.z * pw.y, -g.z * pw.x + g.x * pw.z,
+                  -g.x * pw.y + g.y * pw.x};
+        for (int i = 0; i < 6; ++i) {
+          for (int j = 0; j < 6; ++j) A[i * 6 + j] += (double)(J[i] * J[j]);
+          b[i] += (double)(d * J[i]);
+        }
+        err += (double)(d * d);
+        ++count;
+      }
+    }
+  }
+
   // ---------------------------------------------------------- marching cubes
   // SurfelExtractionKernel (meshing/marching_cubes.cu:75-170): cube validity,
   // cube index, and the shared vertices of cut edges.
@@ -1962,6 +1994,15 @@ int orc_gc_recycle(void *hp) {
   int n = 0;
   DISPATCH(h, n = vol->gc_recycle());
   return n;
+}
+
+void orc_point_to_psdf(void *hp, const float *wTc, int fix_j, double *A, double *b, double *err, int *count) {
+  OHandle *h = (OHandle *)hp;
+  DISPATCH(h, {
+    decltype(vol->wTc) m;
+    for (int i = 0; i < 16; ++i) m.e[i] = wTc[i];
+    vol->point_to_psdf(m, fix_j != 0, A, b, *err, *count);
+  });
 }
 
 void orc_huber_init(void *hp) {

@@ -80,6 +80,8 @@ def lib():
         L.orc_denoise_tv.argtypes = [vp, C.c_float, C.c_int]
         L.orc_get_depth.argtypes = [vp, f32p]
         L.orc_huber_init.argtypes = [vp]
+        L.orc_point_to_psdf.argtypes = [vp, f32p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double), i32p]
         L.orc_huber_iterate.argtypes = [vp, C.c_float, C.c_float, C.c_float, C.c_int, C.POINTER(C.c_double)]
         L.orc_debug_ray.argtypes = [vp, f32p, C.c_int, C.c_int, C.POINTER(C.c_double)]
         L.orc_raycast_backward.argtypes = [vp, f32p, f32p, f32p, C.POINTER(C.c_double)]
@@ -262,6 +264,15 @@ class Oracle:
 
     def denoise_tv(self, lam=0.1, iterations=20):
         self.L.orc_denoise_tv(self.h, float(lam), int(iterations))
+
+    def point_to_psdf(self, wTc, fix_jacobian=False):
+        """PointToSurface normal equations at wTc over the current frame:
+        (A[6, 6], b[6], err, count), sums in double."""
+        m = f32(wTc).reshape(16)
+        A, b, e = (C.c_double * 36)(), (C.c_double * 6)(), C.c_double(0)
+        n = C.c_int32(0)
+        self.L.orc_point_to_psdf(self.h, _p(m, C.c_float), 1 if fix_jacobian else 0, A, b, C.byref(e), C.byref(n))
+        return np.array(list(A)).reshape(6, 6), np.array(list(b)), e.value, n.value
 
     def huber_tv_init(self):
         """PrimalDualInit over the current candidate blocks."""

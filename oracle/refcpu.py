@@ -6,7 +6,7 @@ the reference tree, so it runs only where that tree is present (this is how
 tests/golden/ fixtures are produced; see tests/golden/make_golden.py).
 ``RefCPU`` drives the reference's stages (AllocBlockArray,
 CollectBlocksInFrustum, UpdateBlocksSimple / Bayesian, MarchingCubes, GC,
-RayCaster::Cast, PrimalDualInit / Iterate) with the reference's launch shapes, one emulated CUDA
+RayCaster::Cast, PrimalDualInit / Iterate, PointToSurface) with the reference's launch shapes, one emulated CUDA
 thread at a time.
 """
 from __future__ import annotations
@@ -72,6 +72,7 @@ def lib():
         L.ref_inverse.argtypes = [f32p, f32p]
         L.ref_cube_indices.argtypes = [vp, C.c_int, i32p, C.POINTER(C.c_uint8)]
         L.ref_pd_init.argtypes = [vp]
+        L.ref_point_to_psdf.argtypes = [vp, f32p, f32p, f32p, f32p, i32p]
         L.ref_set_candidates.restype = C.c_int
         L.ref_set_candidates.argtypes = [vp, C.c_int, i32p]
         L.ref_pd_iterate.argtypes = [vp, C.c_float, C.c_float, C.c_float, f32p]
@@ -134,6 +135,15 @@ class RefCPU:
     def set_candidates(self, pos):
         pos = np.ascontiguousarray(pos, np.int32).reshape(-1, 3)
         return self.L.ref_set_candidates(self.h, len(pos), _p(pos, C.c_int32))
+
+    def point_to_psdf(self, wTc):
+        """PointToSurface at pose wTc: (A[6, 6], b[6], err, count), float sums."""
+        m = np.ascontiguousarray(wTc, np.float32).reshape(16)
+        A, b, e = np.zeros(36, np.float32), np.zeros(6, np.float32), np.zeros(1, np.float32)
+        n = C.c_int32(0)
+        self.L.ref_point_to_psdf(self.h, _p(m, C.c_float), _p(A, C.c_float), _p(b, C.c_float), _p(e, C.c_float),
+                                 C.byref(n))
+        return A.reshape(6, 6), b, float(e[0]), n.value
 
     def pd_init(self):
         self.L.ref_pd_init(self.h)

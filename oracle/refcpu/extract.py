@@ -24,6 +24,7 @@ SOURCES = [
     ("src/visualization/ray_caster.cu", ()),
     ("src/mapping/recycle.cu", ()),
     ("src/optimize/primal_dual.cu", ()),
+    ("src/localizing/point_to_psdf.cu", ()),
 ]
 
 
@@ -31,6 +32,10 @@ def functions(text):
     """Yield (name, start, end) of top-level __global__/__device__ functions."""
     for m in re.finditer(r"^(__global__|__device__)\b", text, re.M):
         start = m.start()
+        # a template header on the line before belongs to the function
+        prev = text.rfind("\n", 0, max(start - 1, 0))
+        if text[prev + 1:start].lstrip().startswith("template"):
+            start = prev + 1
         brace = text.find("{", start)
         semi = text.find(";", start)
         if brace < 0 or (0 <= semi < brace):

@@ -11,7 +11,8 @@
 // (mapping/allocate.cu:101-125, core/collect_block_array.cu:245-276,
 // mapping/update_simple.cu:79-108, mapping/update_bayesian.cu:372-433,
 // meshing/marching_cubes.cu:326-382, mapping/recycle.cu:183-274,
-// visualization/ray_caster.cu:190-209, optimize/primal_dual.cu:146-223).  Every emulated CUDA thread runs
+// visualization/ray_caster.cu:190-209, optimize/primal_dual.cu:146-223,
+// localizing/point_to_psdf.cu:86-147).  Every emulated CUDA thread runs
 // to completion (or to its next __syncthreads) before the next one starts.
 #include "cuda_host.h"
 #include "helper_math.h"
@@ -518,6 +519,29 @@ void ref_pd_iterate(void *h, float lambda, float sigma, float tau, float *err) {
   });
   launch(D3(n), D3(BLOCK_SIZE), false,
          [&] { PrimalDualIteratePass2Kernel(r->cand, r->blocks, r->ht, r->gh, lambda, sigma, tau); });
+}
+
+// PointToSurface (localizing/point_to_psdf.cu:86-147): the tracker's normal
+// equations at the pose wTc over the current depth frame, 16x16 CTAs, the
+// accumulators in host memory.
+void ref_point_to_psdf(void *h, const float *wTc, float *A, float *b, float *err, int *count) {
+  Ref *r = (Ref *)h;
+  float4x4 T;
+  for (int i = 0; i < 16; ++i) T.entries[i] = wTc[i];
+  mat6x6 mA;
+  mat6x1 mb;
+  mA.setZero();
+  mb.setZero();
+  float e = 0.0f;
+  int c = 0;
+  const unsigned t = 16;
+  launch(D3((r->sp.width + t - 1) / t, (r->sp.height + t - 1) / t), D3(t, t), false, [&] {
+    PointToSurfaceKernel(r->blocks, r->sd, r->sp, T, r->ht, r->gh, &mA, &mb, &e, &c);
+  });
+  for (int i = 0; i < 36; ++i) A[i] = mA.entries[i];
+  for (int i = 0; i < 6; ++i) b[i] = mb.entries[i];
+  *err = e;
+  *count = c;
 }
 
 // Live blocks: pos[3n] and voxel fields [512n] in hash-entry order.

@@ -69,6 +69,10 @@ class OracleRunner:
     def inlier(self):
         return self.o.inlier()
 
+    def track_equations(self, depth, T):
+        self.o.frame_set(depth, T)
+        return self.o.point_to_psdf(T, fix_jacobian=False)
+
 
 class GpuRunner:
     def __init__(self, params):
@@ -108,6 +112,10 @@ class GpuRunner:
 
     def inlier(self):
         return self.v.inlier()
+
+    def track_equations(self, depth, T):
+        self.v.set_frame(depth, T)
+        return self.v.point_to_psdf(T, reference_jacobian=True)
 
 
 def rows(pos, field, want):
@@ -199,3 +207,22 @@ def check_huber(impl):
     before = rows(fx["pre_pos"], fx["pre_sdf"], fx["cand"])
     assert np.count_nonzero(fx["post_sdf"] != before) > 5000
     return h.sdf(fx["cand"]), fx["post_sdf"], before
+
+
+def check_track(runner_cls):
+    """The reference's tracker equations (PointToSurface, with its J[2] =
+    dD/dx) at the fixture's poses over the simple chain's map: the same
+    pixels contribute; A, b and err agree to float summation (the reference
+    adds floats one by one)."""
+    fx, sc = load("track_room96.npz"), load("simple_room96.npz")
+    r = runner_cls(simple_params())
+    for d, T in zip(sc["depth"], sc["poses"]):
+        r.frame(d, T)
+    for k, T in enumerate(fx["poses"]):
+        A, b, e, n = r.track_equations(fx["depth"], T)
+        assert n == fx["count"][k] and n > 1000
+        assert np.abs(A - fx["A"][k]).max() <= 1e-5 * np.abs(fx["A"][k]).max()
+        assert np.abs(b - fx["b"][k]).max() <= 1e-5 * np.abs(fx["b"][k]).max()
+        assert abs(e - fx["err"][k]) <= 1e-5 * fx["err"][k]
+        # the reference's Jacobian repeats dD/dx in place of dD/dz
+        np.testing.assert_array_equal(A[:, 2], A[:, 0])

@@ -19,6 +19,9 @@ committed, so tests never need the tree.
                      simple chain's last candidates: the cluster's and its
                      face neighbours' sdf and weight before, the cluster's
                      sdf after, the two error sums of every iteration
+  track_room96.npz   PointToSurface (localizing/point_to_psdf.cu) on the
+                     simple chain's map with frame 18's depth at two poses
+                     off the true one: A, b, err and count
 
 Both use params.compat_arithmetic = 1 (the reference's single-precision
 formulas as written).  Allocation is repeated until no block is added, which
@@ -149,6 +152,40 @@ def run_huber(ref_mod, p, depth, poses):
                 hparams=np.array([HUBER["lam"], HUBER["sigma"], HUBER["tau"], HUBER["iterations"]], np.float32))
 
 
+TRACK_FRAME = 18
+TRACK_XI = [[0.01, -0.005, 0.008, 0.01, -0.008, 0.005], [-0.02, 0.012, -0.01, -0.015, 0.01, 0.02]]
+
+
+def track_case():
+    """Frame 18 of the simple trajectory and the poses the fixture uses."""
+    from meshhashing_gb300.pose import left_update
+    wl = scene.small_circle(60)
+    f = 262.5 * 96 / 320
+    wl.camera = scene.Camera(96, 72, f, f, 47.5, 35.5)
+    T = wl.pose(TRACK_FRAME).astype(np.float64)
+    poses = np.stack([left_update(T, np.array(x)).astype(np.float32) for x in TRACK_XI])
+    return wl.frame(TRACK_FRAME), T.astype(np.float32), poses
+
+
+def run_track(ref_mod, p, depth, poses):
+    r = ref_mod.RefCPU(p)
+    for d, T in zip(depth, poses):
+        r.frame_set(d, T)
+        r.alloc(True)
+        r.collect()
+        r.integrate_simple()
+        r.mesh()
+        r.gc_low_surfel()
+    d18, T18, tp = track_case()
+    out = {"A": [], "b": [], "err": [], "count": []}
+    for T in tp:
+        r.frame_set(d18, T)
+        A, b, e, n = r.point_to_psdf(T)
+        out["A"].append(A), out["b"].append(b), out["err"].append(e), out["count"].append(n)
+    return dict(depth=d18, pose_true=T18, poses=tp, A=np.stack(out["A"]), b=np.stack(out["b"]),
+                err=np.array(out["err"], np.float32), count=np.array(out["count"], np.int32))
+
+
 def rows(pos, field, want):
     idx = {tuple(q): i for i, q in enumerate(pos.tolist())}
     return np.stack([field[idx[tuple(q)]] for q in np.asarray(want).tolist()])
@@ -164,7 +201,8 @@ def main():
     np.savez_compressed(os.path.join(HERE, "psdf_room96.npz"), **run_psdf(refcpu, p, depth, poses))
     p, depth, poses = simple_case()
     np.savez_compressed(os.path.join(HERE, "huber_room96.npz"), **run_huber(refcpu, p, depth, poses))
-    for f in ("simple_room96.npz", "psdf_room96.npz", "huber_room96.npz"):
+    np.savez_compressed(os.path.join(HERE, "track_room96.npz"), **run_track(refcpu, p, depth, poses))
+    for f in ("simple_room96.npz", "psdf_room96.npz", "huber_room96.npz", "track_room96.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

@@ -41,6 +41,10 @@ class _OracleHuber:
         return _golden.rows(pos, s, cand)
 
 
+def test_oracle_matches_reference_tracker_equations(built):
+    _golden.check_track(_golden.OracleRunner)
+
+
 def test_oracle_matches_reference_huber_tv(built):
     import numpy as np
     got, want, _ = _golden.check_huber(_OracleHuber)
@@ -66,4 +70,8 @@ def test_fixtures_regenerate_from_reference(built, tmp_path):
     out = mg.run_huber(refcpu, p, depth, poses)
     fx = _golden.load("huber_room96.npz")
     for k in ("pre_pos", "pre_sdf", "pre_w", "cand", "post_sdf", "errs"):
+        np.testing.assert_array_equal(out[k], fx[k])
+    out = mg.run_track(refcpu, p, depth, poses)
+    fx = _golden.load("track_room96.npz")
+    for k in ("depth", "poses", "A", "b", "err", "count"):
         np.testing.assert_array_equal(out[k], fx[k])

@@ -22,6 +22,10 @@ def test_gpu_matches_reference_psdf_chain(built):
     _golden.check_psdf(_golden.GpuRunner)
 
 
+def test_gpu_matches_reference_tracker_equations(built):
+    _golden.check_track(_golden.GpuRunner)
+
+
 class _GpuHuber:
     def __init__(self, params, pos, sdf, w, cand):
         import numpy as np

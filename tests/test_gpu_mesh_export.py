@@ -1,7 +1,7 @@
-"""Dense mesh export (mh_mesh_compact, mh_write_ply) against the mesh held in
-the volume's pools (mh_dump_mesh): the same triangles, as triples of vertex
-positions; only referenced vertices; the same arrays on a second call; and
-the PLY file holds exactly those arrays."""
+"""Dense mesh export (mh_mesh_compact, mh_write_ply, mh_write_obj) against the
+mesh held in the volume's pools (mh_dump_mesh): the same triangles, as
+triples of vertex positions; only referenced vertices; the same arrays on a
+second call; and the PLY and OBJ files hold exactly those arrays."""
 import numpy as np
 import pytest
 
@@ -57,3 +57,10 @@ def test_compact_matches_pools_and_ply(built, tmp_path):
     assert np.array_equal(vrec[:, :3], pos) and np.array_equal(vrec[:, 3:], nrm)
     frec = np.frombuffer(body[len(pos) * 24:], np.dtype([("n", "u1"), ("i", "<i4", (3,))]))
     assert np.all(frec["n"] == 3) and np.array_equal(frec["i"], tri)
+    obj = tmp_path / "mesh.obj"
+    v.write_obj(obj)
+    lines = obj.read_text().splitlines()
+    vl = np.array([[float(x) for x in ln.split()[1:]] for ln in lines if ln.startswith("v ")], np.float32)
+    nl = np.array([[float(x) for x in ln.split()[1:]] for ln in lines if ln.startswith("vn ")], np.float32)
+    fl = np.array([[int(x.split("//")[0]) for x in ln.split()[1:]] for ln in lines if ln.startswith("f ")])
+    assert np.array_equal(vl, pos) and np.array_equal(nl, nrm) and np.array_equal(fl - 1, tri)
