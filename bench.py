@@ -56,19 +56,22 @@ def gen_frames(indices, n_total, w=640, h=480, procs=None):
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle samples during the timed region."""
+    """nvidia-smi clock/throttle samples every 50 ms, each with its own
+    timestamp, so the summary keeps exactly the samples taken inside the
+    timed region."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self):
         self.rows, self.proc, self.thread = [], None, None
 
-    def start(self):
+    def start(self, interval_ms=50):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                                          "-lms", str(interval_ms)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
         except (OSError, FileNotFoundError):
             self.proc = None
             return
@@ -76,10 +79,24 @@ class ClockSampler:
         self.thread.start()
 
     def _read(self):
+        import datetime
         for line in self.proc.stdout:
-            self.rows.append([c.strip() for c in line.split(",")])
+            r = [c.strip() for c in line.split(",")]
+            if len(r) < 10:
+                continue
+            ts = None
+            for fmt in ("%Y/%m/%d %H:%M:%S.%f", "%Y/%m/%d %H:%M:%S"):
+                try:
+                    ts = datetime.datetime.strptime(r[0], fmt).timestamp()
+                    break
+                except ValueError:
+                    pass
+            self.rows.append([ts if ts is not None else time.time()] + r[1:])
 
-    def stop(self):
+    def stop(self, window, loaded):
+        """Summary of the samples inside `window` (wall-clock seconds); when
+        the timed region was shorter than the sampling interval, of those in
+        `loaded` (the timed region and the same workload's passes after it)."""
         if self.proc is None:
             return None
         self.proc.terminate()
@@ -87,24 +104,30 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        if not self.rows:
+        if self.thread is not None:
+            self.thread.join(timeout=5)
+        span = "timed region"
+        rows = [r for r in self.rows if window[0] <= r[0] <= window[1]]
+        if not rows:
+            span = "timed region and the profiled pass of the same workload after it"
+            rows = [r for r in self.rows if loaded[0] <= r[0] <= loaded[1]]
+        if not rows:
             return None
         by_gpu = {}
-        for r in self.rows:
-            if len(r) >= 9:
-                by_gpu.setdefault(r[0], []).append(r)
+        for r in rows:
+            by_gpu.setdefault(r[1], []).append(r)
 
-        def pw(rows):
-            v = [float(r[3]) for r in rows if r[3].replace(".", "", 1).isdigit()]
+        def pw(rs):
+            v = [float(r[4]) for r in rs if r[4].replace(".", "", 1).isdigit()]
             return float(np.median(v)) if v else 0.0
         gpu = max(by_gpu, key=lambda g: pw(by_gpu[g]))
         rows = by_gpu[gpu]
-        sm = [float(r[1]) for r in rows if r[1].isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].isdigit()]
+        sm = [float(r[2]) for r in rows if r[2].isdigit()]
+        mx = [float(r[3]) for r in rows if r[3].isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[6 + k].lower().startswith("active")})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "gpu": gpu, "samples": len(rows)}
+                "reasons": reasons, "gpu": gpu, "samples": len(rows), "interval_ms": 50, "span": span}
 
 
 def workload_params(capacity_log2=21):
@@ -470,7 +493,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--prefuse", type=int, default=40)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-frames", type=int, default=3)
+    ap.add_argument("--cpu-frames", type=int, default=16,
+                    help="frames of the FP64 oracle CPU baseline (about 10 s on 16 cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=64,
                     help="scenes of the batched-vs-plain measurement (0: skip it)")
@@ -534,17 +558,19 @@ def main():
 
     sampler = ClockSampler()
     sampler.start()
+    time.sleep(0.3)                     # nvidia-smi is sampling before the timed region starts
     barrier()
     l0 = launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    w0 = time.time()
     e0.record()
     for i in range(P + W, P + W + K):
         step(i)
     e1.record()
     barrier()
+    w1 = time.time()
     launches = launch_count() - l0
     ms = e0.elapsed_time(e1)
-    clocks = sampler.stop()
     # per-stage times: a second pass over the next K frames with CUDA events
     # around every stage (kept out of the timed region above)
     s0 = vol.stats()
@@ -555,6 +581,7 @@ def main():
     prof = vol.profile_read()
     vol.profile(False)
     s1 = vol.stats()
+    clocks = sampler.stop((w0, w1), (w0, time.time()))
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
