@@ -195,9 +195,13 @@ int mh_integrate_frame(mh_volume *v, const float *depth, int depth_on_device,
                        float *ray_depth, float *ray_vertex4, float *ray_normal4,
                        int outputs_on_device, void *stream);
 
-/* Synchronises `stream`, then reads the counters and the sticky error word. */
+/* Synchronises `stream`, then reads the counters and the sticky error word:
+ * the counts the reference reads back or logs (EntryArray::count(),
+ * core/entry_array.h:20; heap and mesh counters, core/hash_table.h,
+ * core/mesh.h; engine/logging_engine.cc:61-93). */
 int mh_stats_get(mh_volume *v, mh_stats *out, void *stream);
-/* Clears the sticky error word. */
+/* Clears the sticky error word (no counterpart: the reference exits through
+ * checkCudaErrors or printf()s device-side failures). */
 int mh_clear_error(mh_volume *v, void *stream);
 
 /* Host copies of state (synchronising).  Blocks are returned in pool order:
@@ -207,16 +211,23 @@ int mh_clear_error(mh_volume *v, void *stream);
 int mh_dump_blocks(mh_volume *v, int max_blocks, int32_t *pos, float *sdf,
                    float *weight, float *a, float *b, int *n_out);
 /* Overwrite the voxel state of existing blocks (same layout as the dump);
- * blocks not present are inserted.  Used to hand a state to the stages. */
+ * blocks not present are inserted.  Used to hand a state to the stages (no
+ * counterpart; the reference's block replay is LoggingEngine's,
+ * engine/logging_engine.cc:101-233). */
 int mh_load_blocks(mh_volume *v, int n, const int32_t *pos, const float *sdf,
                    const float *weight, const float *a, const float *b);
-/* Current candidate list as block coordinates pos[3n]. */
+/* Current candidate list as block coordinates pos[3n] (EntryArray,
+ * core/entry_array.h:10-50, as CollectBlocksInFrustum leaves it). */
 int mh_dump_candidates(mh_volume *v, int max_n, int32_t *pos, int *n_out);
-/* Replace the candidate list by the given existing blocks. */
+/* Replace the candidate list by the given existing blocks (the reference's
+ * stages read whatever EntryArray holds, core/entry_array.h:10-50). */
 int mh_set_candidates(mh_volume *v, int n, const int32_t *pos);
-/* Inlier-ratio image (width x height floats). */
+/* Inlier-ratio image (width x height floats; SensorData::inlier_ratio,
+ * sensor/rgbd_sensor.h:16-40, after PredictOutlierRatio). */
 int mh_dump_inlier(mh_volume *v, float *out);
-/* Current (preprocessed) depth frame (width x height floats). */
+/* Current (preprocessed) depth frame (width x height floats; the depth
+ * texture of SensorData after ConvertDepthFormatKernel,
+ * sensor/preprocess.cu:25-42). */
 int mh_dump_depth(mh_volume *v, float *out);
 
 /* Mesh state in pool-independent form.  For every live vertex slot:
@@ -227,10 +238,12 @@ int mh_dump_depth(mh_volume *v, float *out);
  * Pass NULL arrays to query counts only. */
 int mh_dump_mesh(mh_volume *v, int max_vertices, int32_t *vkeys, float *vdata,
                  int max_triangles, int32_t *tris, int *n_vertices, int *n_triangles);
-/* Per-voxel cube index of a block list (curr_cube_idx), 512 per block. */
+/* Per-voxel cube index of a block list (MeshUnit::curr_cube_idx,
+ * core/voxel.h:27-60), 512 per block. */
 int mh_dump_cubes(mh_volume *v, int n, const int32_t *pos, uint8_t *cube_idx);
-/* Block bookkeeping for garbage collection: life_count_down, inner and
- * boundary surfel counts, and the GC flag of each candidate. */
+/* Block bookkeeping for garbage collection (Block, core/block.h:15-40):
+ * life_count_down, inner and boundary surfel counts; and the GC flag of each
+ * candidate (EntryArray::flag, core/entry_array.h:29-31). */
 int mh_dump_block_meta(mh_volume *v, int n, const int32_t *pos, int32_t *life,
                        int32_t *inner, int32_t *boundary);
 int mh_dump_flags(mh_volume *v, int max_n, uint8_t *flags, int *n_out);
@@ -252,10 +265,10 @@ int mh_profile_enable(mh_volume *v, int enable);
 /* Synchronises, returns the accumulated ms and call counts per stage since
  * the last read, and resets them. */
 int mh_profile_read(mh_volume *v, double ms[MH_STAGE_COUNT], int calls[MH_STAGE_COUNT]);
-/* Number of kernels this library has launched in the process. */
+/* Number of kernels this library has launched in the process (no
+ * counterpart; a measurement aid). */
 uint64_t mh_launch_count(void);
 
-/* Teschner hash of a block position (core/hash_table.h:259-269). */
 /* Dense copy of the mesh (CompressMesh, visualization/compress_mesh.cu:10-172):
  * the vertices referenced by live triangles (position and normal, 3 floats
  * each) and the triangles with their indices remapped, in pool order, so the
@@ -309,7 +322,9 @@ int mh_huber_tv_iterate(mh_volume *v, float lambda, float sigma, float tau, int 
  * writes dL/dxi (host).  Synchronising. */
 int mh_raycast_backward(mh_volume *v, const float cTw[16], const float *dL_ddepth, const float *dL_dnormal4,
                         float *grad_sdf, double dL_dxi[6], void *stream);
-/* Gauss-Newton normal equations of frame-to-model alignment, driven by the
+/* No reference counterpart (the reference tracks with the point-to-PSDF
+ * residual below, engine/main_engine.cc:70-98).
+ * Gauss-Newton normal equations of frame-to-model alignment, driven by the
  * raycast: for every pixel with a hit, an observation (> 0, finite) and
  * |rendered - observed depth| < max_residual, the observed point on the
  * pixel's ray is compared with the tangent plane of the model at the hit
@@ -347,7 +362,8 @@ int mh_point_to_psdf_normal_equations(mh_volume *v, const float wTc[16], int ref
 int mh_track_point_to_psdf(mh_volume *v, float wTc[16], int iterations, float lambda, int reference_jacobian,
                            double *final_err, int *final_count, void *stream);
 /* Like mh_dump_blocks for a caller's device field laid out like the voxel
- * storage (value_capacity x 512 floats), e.g. the grad_sdf above. */
+ * storage (value_capacity x 512 floats), e.g. the grad_sdf above (no
+ * counterpart). */
 int mh_dump_block_field(mh_volume *v, const float *field, int max_blocks, int32_t *pos, float *out, int *n_out);
 
 /* ------------------------------------------------------------------ batches
@@ -399,9 +415,13 @@ int mh_batch_tuning_times(mh_batch *b, double ray_ms[3], double integrate_ms[3])
  * -1 before any; the raycast entry covers the raycast only */
 int mh_batch_stage_times(mh_batch *b, double ms[MH_STAGE_COUNT]);
 
+/* Teschner hash of a block position (HashBucketForBlockPos,
+ * core/hash_table.h:259-269). */
 uint32_t mh_hash_bucket(int32_t x, int32_t y, int32_t z, uint32_t bucket_count);
-/* Bytes the last frame's stages needed by the algorithmic model (see the
- * design notes); per stage: [alloc, collect, integrate, predict, mesh, raycast]. */
+/* Bytes the last frame's stages needed by the algorithmic model (no
+ * counterpart; a measurement aid): the voxel fields and image pixels each
+ * stage must read and write for the blocks and pixels it visited, per stage
+ * [alloc, collect, integrate, predict, mesh, raycast]. */
 int mh_bytes_model(mh_volume *v, double out[6]);
 
 #ifdef __cplusplus
