@@ -108,8 +108,8 @@ def test_integrate_simple_exact(built):
     print(f"simple update vs FP64: max |dsdf| = {worst_s:.3e} m, max rel dw = {worst_w:.3e}")
 
 
-def _psdf_chain(v, o32, wl, frames, with_checks=True):
-    stats = {"inlier_max_ulp": 0, "sdf_rel": 0.0, "w_rel": 0.0}
+def _psdf_chain(v, o32, wl, frames, with_checks=True, o64=None):
+    stats = {"inlier_max_ulp": 0, "sdf_rel": 0.0, "w_rel": 0.0, "sdf64_abs": 0.0, "w64_rel": 0.0, "ab64_rel": 0.0}
     for i in frames:
         d, T = wl.frame(i), wl.pose(i)
         v.set_frame(d, T)
@@ -117,16 +117,34 @@ def _psdf_chain(v, o32, wl, frames, with_checks=True):
         v.collect_blocks_in_frustum()
         cand = v.candidates()
         if with_checks:
-            hand_over(v, o32, with_mesh=True)
-            o32.frame_set(d, T)
-            o32.set_candidates(cand)
+            for o in (o32,) + ((o64,) if o64 is not None else ()):
+                hand_over(v, o, with_mesh=True)
+                o.frame_set(d, T)
+                o.set_candidates(cand)
         v.predict_outlier_ratio()
         if with_checks:
             o32.predict_inlier()
             gi, oi = v.inlier(), o32.inlier()
             stats["inlier_max_ulp"] = max(stats["inlier_max_ulp"], int(ulp_diff(gi, oi).max()))
             o32.set_inlier(gi)
+            if o64 is not None:
+                o64.set_inlier(gi)
         v.update_blocks_bayesian()
+        if with_checks and o64 is not None:
+            # the same update in double from the same state and inlier ratios
+            o64.integrate_psdf()
+            gpos, gf = v.dump_blocks()
+            p64, s64, w64, a64, b64 = o64.blocks()
+            g, o, _ = align(gpos, gf["sdf"], p64, s64)
+            stats["sdf64_abs"] = max(stats["sdf64_abs"], float(np.abs(g - o).max()) if g.size else 0.0)
+            g, o, _ = align(gpos, gf["w"], p64, w64)
+            m = o > 0
+            stats["w64_rel"] = max(stats["w64_rel"], float((np.abs(g - o)[m] / o[m]).max()) if m.any() else 0.0)
+            for key, ofield in (("a", a64), ("b", b64)):
+                g, o, _ = align(gpos, gf[key], p64, ofield)
+                m = np.abs(o) > 1e-3
+                if m.any():
+                    stats["ab64_rel"] = max(stats["ab64_rel"], float((np.abs(g - o)[m] / np.abs(o[m])).max()))
         if with_checks:
             o32.integrate_psdf()
             gpos, gf = v.dump_blocks()
@@ -148,10 +166,13 @@ def test_psdf_predict_and_update(built):
     o32 = Oracle(p, fp64=False)
     # build up a surface with meshed vertices first, then check stage-wise
     _psdf_chain(v, o32, wl, range(0, 12), with_checks=False)
-    st = _psdf_chain(v, o32, wl, range(12, 18), with_checks=True)
+    st = _psdf_chain(v, o32, wl, range(12, 18), with_checks=True, o64=Oracle(p, fp64=True))
     # expf differs by a few ulp between the CUDA and host math libraries
     assert st["inlier_max_ulp"] <= 64, st
     assert st["sdf_rel"] < 1e-4 and st["w_rel"] < 1e-4, st
+    print(f"PSDF update vs FP64: max |dsdf| = {st['sdf64_abs']:.3e} m, max rel dw = {st['w64_rel']:.3e}, "
+          f"max rel da/db = {st['ab64_rel']:.3e}")
+    assert st["sdf64_abs"] < 1e-5 and st["w64_rel"] < 1e-4, st
     assert v.stats()["error"] == 0
 
 
@@ -210,6 +231,7 @@ def test_marching_cubes_topology_exact(built):
             if common:
                 e64 = max(float(np.abs(gverts[k][:3] - overts[k][:3]).max()) for k in common) / p.voxel_size
                 assert e64 < 1e-4, e64
+                print(f"vertex positions vs FP64: max error = {e64:.3e} voxel over {len(common)} vertices")
             life, inner, bnd = v.block_meta(cand)
             _, oin, obnd, _ = o.block_meta(cand)
             np.testing.assert_array_equal(inner, oin)
