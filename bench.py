@@ -409,9 +409,15 @@ def run_stream(frames, poses):
     import torch
     from meshhashing_gb300 import Volume, config, scene
     wl = scene.floor_plan(2000)
-    p = config.params_for(wl, voxel_size=0.005, truncation=0.015, value_capacity=1 << 22, bucket_count=1 << 22,
-                          max_vertex_count=1 << 23, max_triangle_count=1 << 23, overflow_capacity=1 << 20,
-                          mesh_page_capacity=1 << 17)
+    # 12 M blocks (98 GB of voxels): the walk's 5 % outliers, up to 5 m along
+    # the rays, end up allocating most of the free space in and around the
+    # building (7.7 M blocks live after the 2000 frames).  At 1.8 blocks per
+    # bucket (2^22 buckets of 4 slots) the Teschner hash overfills some
+    # buckets past 4 + 7 entries, so overflow chains may grow to 32 here
+    # (linked_list_size, a HashParams knob; the reference's default is 7).
+    p = config.params_for(wl, voxel_size=0.005, truncation=0.015, value_capacity=12_000_000, bucket_count=1 << 22,
+                          max_vertex_count=1 << 23, max_triangle_count=1 << 23, overflow_capacity=1 << 22,
+                          mesh_page_capacity=1 << 19, linked_list_size=32)
     vol = Volume(p)
     dev = torch.from_numpy(np.stack(frames)).cuda()
     rd = torch.empty((p.height, p.width), dtype=torch.float32, device="cuda")
@@ -436,7 +442,8 @@ def run_stream(frames, poses):
             "ms_per_frame": ms / len(frames), "blocks_allocated": s["blocks_allocated"], "blocks_peak": int(peak),
             "gc_freed_blocks": s["gc_freed_blocks"], "triangles": s["triangles_allocated"],
             "vertices": s["vertices_allocated"], "candidates_per_frame": s["candidate_sum"] / max(s["mesh_passes"], 1),
-            "error": s["error"], "dropped_inserts": s["dropped_inserts"],
+            "error": s["error"], "dropped_inserts": s["dropped_inserts"], "overflow_used": s["overflow_used"],
+            "mesh_pages_used": s["mesh_pages_used"], "block_capacity": p.value_capacity,
             "note": "frames 0..%d of the 2000-frame walk, the map growing from empty; the stats() reads "
                     "every 50 frames are inside the timed region" % (len(frames) - 1)}
 
