@@ -9,12 +9,15 @@
 // over pairs of valid pixels only (invalid pixels are holes with Neumann
 // boundaries and stay invalid), tau = sigma = 1/sqrt(8).
 //
-// One launch per iteration: each thread recomputes the dual update of its own
-// pixel and of its left and upper neighbours (the ones its divergence needs)
-// from the previous iterate, so the dual and primal steps fuse into a single
-// pass with no grid-wide barrier.  The recomputed neighbour values are
-// bit-identical to the neighbours' own, so the result does not depend on the
-// tiling.
+// Two forms, bit-identical to each other:
+//  * k_tv_iter, one launch per iteration (the batch twin and the
+//    allocation-free entry point): each thread recomputes the dual update of
+//    its own pixel and of its left and upper neighbours (the ones its
+//    divergence needs) from the previous iterate, so the dual and primal
+//    steps fuse into a single pass with no grid-wide barrier;
+//  * k_tv_tile (a volume's frames): ten iterations per launch on a 64 x 32
+//    tile held in shared memory with a 10-pixel halo, so 20 iterations take
+//    2 launches instead of 22.
 #include "mh_internal.cuh"
 #include "mh_kernels.h"
 #include "mh_batch.cuh"
@@ -121,8 +124,147 @@ __global__ void k_tv_out_b(const Scene *t, int n, int iterations) {
   });
 }
 
+// ------------------------------------------------------------------ tiled
+// Up to TV_K iterations per launch for one TV_TW x TV_TH tile of pixels: the
+// tile and a TV_K-pixel halo sit in shared memory, every iteration runs the
+// dual step over the whole region, then the primal step, and values go stale
+// by one pixel per iteration from the region's edge inwards, so the tile's
+// own pixels stay exact through TV_K iterations.  Each value is computed by
+// the same expressions as tv_iter_body (the dual of a neighbour is the
+// neighbour's own new dual), so the result is bit-identical to running
+// k_tv_iter once per iteration.  The first launch initialises from the depth
+// frame (as k_tv_init), the last writes the frame back (as k_tv_out); between
+// launches the iterate goes through the ping-pong planes.
+#define TV_TW 64
+#define TV_TH 32
+#define TV_K 10
+#define TV_RW (TV_TW + 2 * TV_K)
+#define TV_RH (TV_TH + 2 * TV_K)
+#define TV_RN (TV_RW * TV_RH)
+constexpr size_t kTvTileSmem = sizeof(float) * 5 * TV_RN;
+
+struct TvTile {
+  const float *depth_in;  // first launch: the depth frame (metres); else null
+  float *depth_out;       // last launch: the frame to write; else null
+  float *f;               // input plane (written by the first launch)
+  const float *u, *ub, *px, *py;  // iterate in (unused by the first launch)
+  float *u2, *ub2, *px2, *py2;    // iterate out (unused by the last launch)
+  int W, H, iters;
+  float lambda;
+};
+
+__global__ void __launch_bounds__(1024) k_tv_tile(TvTile b) {
+  extern __shared__ float sm[];
+  float *sf = sm, *su = sm + TV_RN, *sub = sm + 2 * TV_RN, *spx = sm + 3 * TV_RN, *spy = sm + 4 * TV_RN;
+  const float tau = 0.35355339059327373f, sigma = 0.35355339059327373f;
+  const int x0 = blockIdx.x * TV_TW - TV_K, y0 = blockIdx.y * TV_TH - TV_K;
+  const float NI = -__int_as_float(0x7f800000);
+  for (int r = threadIdx.x; r < TV_RN; r += blockDim.x) {
+    const int gx = x0 + r % TV_RW, gy = y0 + r / TV_RW;
+    float f = 0.0f, u = 0.0f, ub = 0.0f, px = 0.0f, py = 0.0f;
+    if (gx >= 0 && gx < b.W && gy >= 0 && gy < b.H) {
+      const int i = gy * b.W + gx;
+      if (b.depth_in) {
+        const float z = b.depth_in[i];
+        const bool ok = z > 0.0f && z < 1e30f;
+        f = u = ub = ok ? z * 1000.0f : NI;
+      } else {
+        f = b.f[i], u = b.u[i], ub = b.ub[i], px = b.px[i], py = b.py[i];
+      }
+    }
+    sf[r] = f, su[r] = u, sub[r] = ub, spx[r] = px, spy[r] = py;
+  }
+  __syncthreads();
+  for (int it = 0; it < b.iters; ++it) {
+    // dual step (dual_at): forward differences of ub over valid pairs
+    for (int r = threadIdx.x; r < TV_RN; r += blockDim.x) {
+      const int lx = r % TV_RW, ly = r / TV_RW, gx = x0 + lx, gy = y0 + ly;
+      const bool vi = sf[r] > -1e30f;
+      float gxd = 0.0f, gyd = 0.0f;
+      if (vi && gx + 1 < b.W && lx + 1 < TV_RW && sf[r + 1] > -1e30f) gxd = sub[r + 1] - sub[r];
+      if (vi && gy + 1 < b.H && ly + 1 < TV_RH && sf[r + TV_RW] > -1e30f) gyd = sub[r + TV_RW] - sub[r];
+      const float qx = spx[r] + sigma * gxd;
+      const float qy = spy[r] + sigma * gyd;
+      const float nrm = fmaxf(1.0f, sqrtf(qx * qx + qy * qy));
+      spx[r] = qx / nrm;
+      spy[r] = qy / nrm;
+    }
+    __syncthreads();
+    // primal step and extrapolation (tv_iter_body)
+    for (int r = threadIdx.x; r < TV_RN; r += blockDim.x) {
+      if (!(sf[r] > -1e30f)) {
+        su[r] = sf[r];
+        sub[r] = sf[r];
+        continue;
+      }
+      const int lx = r % TV_RW, ly = r / TV_RW, gx = x0 + lx, gy = y0 + ly;
+      const float pxl = (gx > 0 && lx > 0) ? spx[r - 1] : 0.0f;
+      const float pyu = (gy > 0 && ly > 0) ? spy[r - TV_RW] : 0.0f;
+      const float div = (spx[r] - pxl) + (spy[r] - pyu);
+      const float u0 = su[r];
+      const float un = (u0 + tau * div + tau * b.lambda * sf[r]) / (1.0f + tau * b.lambda);
+      su[r] = un;
+      sub[r] = 2.0f * un - u0;
+    }
+    __syncthreads();
+  }
+  for (int k = threadIdx.x; k < TV_TW * TV_TH; k += blockDim.x) {
+    const int lx = TV_K + k % TV_TW, ly = TV_K + k / TV_TW, gx = x0 + lx, gy = y0 + ly;
+    if (gx >= b.W || gy >= b.H) continue;
+    const int r = ly * TV_RW + lx, i = gy * b.W + gx;
+    if (b.depth_in) b.f[i] = sf[r];
+    if (b.depth_out) {
+      b.depth_out[i] = sf[r] > -1e30f ? su[r] * 0.001f : NI;
+    } else {
+      b.u2[i] = su[r], b.ub2[i] = sub[r], b.px2[i] = spx[r], b.py2[i] = spy[r];
+    }
+  }
+}
+
+int launch_denoise_tv_iterated(const Dev &d, float *tv, float lambda, int iterations, cudaStream_t s);
+
 // tv holds 9 planes of W*H floats: f, (u, ub, px, py) x 2
 int launch_denoise_tv(const Dev &d, float *tv, float lambda, int iterations, cudaStream_t s) {
+  const int W = d.p.width, H = d.p.height, n = W * H;
+  if (iterations <= 0) return launch_denoise_tv_iterated(d, tv, lambda, iterations, s);
+  static bool attr_set = false;
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(k_tv_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTvTileSmem) !=
+        cudaSuccess)
+      return MH_ERR_CUDA;
+    attr_set = true;
+  }
+  float *A[4] = {tv + (size_t)n, tv + 2 * (size_t)n, tv + 3 * (size_t)n, tv + 4 * (size_t)n};
+  float *B[4] = {tv + 5 * (size_t)n, tv + 6 * (size_t)n, tv + 7 * (size_t)n, tv + 8 * (size_t)n};
+  const dim3 grid((W + TV_TW - 1) / TV_TW, (H + TV_TH - 1) / TV_TH);
+  int launches = 0;
+  for (int done = 0; done < iterations; done += TV_K) {
+    TvTile b;
+    b.depth_in = done == 0 ? d.depth : nullptr;
+    b.iters = std::min(TV_K, iterations - done);
+    // the first launch reads the frame, so it never writes it back (other
+    // tiles may still be reading their halos)
+    b.depth_out = (done > 0 && done + b.iters == iterations) ? d.depth : nullptr;
+    b.f = tv;
+    b.u = A[0], b.ub = A[1], b.px = A[2], b.py = A[3];
+    b.u2 = B[0], b.ub2 = B[1], b.px2 = B[2], b.py2 = B[3];
+    b.W = W, b.H = H, b.lambda = lambda;
+    k_tv_tile<<<grid, 1024, kTvTileSmem, s>>>(b);
+    ++launches;
+    for (int k = 0; k < 4; ++k) std::swap(A[k], B[k]);
+  }
+  if (iterations <= TV_K) {
+    const int g = min((n + 255) / 256, mh_sm_count() * 8);
+    k_tv_out<<<g, 256, 0, s>>>(tv, A[0], d.depth, n);
+    ++launches;
+  }
+  mh_count_launches(launches);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+
+// the one-launch-per-iteration form (kept for reference timing; the batch
+// path runs its twin k_tv_iter_b)
+int launch_denoise_tv_iterated(const Dev &d, float *tv, float lambda, int iterations, cudaStream_t s) {
   const int W = d.p.width, H = d.p.height, n = W * H;
   const int g = min((n + 255) / 256, mh_sm_count() * 8);
   float *f = tv;
