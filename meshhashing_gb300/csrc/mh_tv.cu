@@ -227,13 +227,11 @@ int launch_denoise_tv_iterated(const Dev &d, float *tv, float lambda, int iterat
 int launch_denoise_tv(const Dev &d, float *tv, float lambda, int iterations, cudaStream_t s) {
   const int W = d.p.width, H = d.p.height, n = W * H;
   if (iterations <= 0) return launch_denoise_tv_iterated(d, tv, lambda, iterations, s);
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(k_tv_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTvTileSmem) !=
-        cudaSuccess)
-      return MH_ERR_CUDA;
-    attr_set = true;
-  }
+  // 87 KB of dynamic shared memory needs the opt-in; the attribute belongs to
+  // the current device, so it is set on every call (it is idempotent)
+  if (cudaFuncSetAttribute(k_tv_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTvTileSmem) !=
+      cudaSuccess)
+    return MH_ERR_CUDA;
   float *A[4] = {tv + (size_t)n, tv + 2 * (size_t)n, tv + 3 * (size_t)n, tv + 4 * (size_t)n};
   float *B[4] = {tv + 5 * (size_t)n, tv + 6 * (size_t)n, tv + 7 * (size_t)n, tv + 8 * (size_t)n};
   const dim3 grid((W + TV_TW - 1) / TV_TW, (H + TV_TH - 1) / TV_TH);
