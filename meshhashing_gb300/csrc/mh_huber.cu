@@ -14,8 +14,8 @@
 //          where w > 2; sdf_bar = 2 sdf - sdf_prev.
 // Differences use face neighbours that exist, are observed and carry the
 // mask; otherwise the gradient (or divergence) is 0, as in the reference.
-// The per-voxel state (7 words) lives in arrays laid out like the voxel
-// storage, allocated on first use; the mask is an epoch stamp, so voxels not
+// The per-voxel state (7 words, plus one for the per-call work list) lives in
+// arrays laid out like the voxel storage, allocated on first use; the mask is an epoch stamp, so voxels not
 // initialised by the latest init read as unmasked.  Every pass runs one
 // thread per candidate voxel over a face-neighbour table that is built once
 // per call, so no pass waits on a hash probe.
@@ -262,6 +262,7 @@ static int pd_ensure(mh_volume *v) {
   st->voxels = nv;
   v->pd = st;
   if (!ok) {
+    cudaGetLastError();  // the failed allocation must not surface at the next launch check
     mh_pd_free(v);
     return MH_ERR_NOMEM;
   }
