@@ -448,6 +448,24 @@ def run_stream(frames, poses):
                     "every 50 frames are inside the timed region" % (len(frames) - 1)}
 
 
+def max_over_ranks(x, world, device):
+    """The largest x over the ranks: replicas run in lockstep between
+    barriers, so the job takes as long as its slowest rank."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, steps, seconds):
+    """Whole-job frames/s: every rank advances its own replica by `steps`
+    frames in `seconds` (the max over ranks)."""
+    return world * steps / seconds
+
+
 def run_cpu_baseline(params, frames, poses, threads=None):
     """FP64 oracle on all host threads, from an empty volume."""
     from oracle import oracle as O
@@ -589,11 +607,8 @@ def main():
     vol.profile(False)
     s1 = vol.stats()
     clocks = sampler.stop((w0, w1), (w0, time.time()))
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * K / (ms / 1000.0)
+    ms = max_over_ranks(ms, world, "cuda")
+    value = job_rate(world, K, ms / 1000.0)
 
     # e2e: host depth in (pinned), raycast depth back to host every frame
     host_in = [torch.from_numpy(f).pin_memory() for f in frames[P + W + 2 * K:P + W + 3 * K]]
@@ -606,12 +621,8 @@ def main():
     for j in range(K):
         step_e2e(j)
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = world * K / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, "cuda")
+    e2e = job_rate(world, K, e2e_s)
     s2 = vol.stats()
 
     passes = max(s1["mesh_passes"] - s0["mesh_passes"], 1)
