@@ -124,7 +124,9 @@ int mh_volume_reset(mh_volume *v, void *stream);
  * (preprocess.cu:10-23) and stores wTc and cTw = inverse(wTc). */
 int mh_frame_set(mh_volume *v, const float *depth, int depth_on_device,
                  const float wTc[16], void *stream);
-/* Same, from uint16 depth scaled by range_factor (preprocess.cu:25-42). */
+/* Same, from raw 16-bit depth scaled by range_factor (preprocess.cu:25-42,
+ * whose source image is a short*): raw values are read as signed, so 32768
+ * and above are negative depths and come out invalid, as in the reference. */
 int mh_frame_set_u16(mh_volume *v, const uint16_t *depth, int depth_on_device,
                      const float wTc[16], void *stream);
 
@@ -175,10 +177,13 @@ int mh_denoise_tv(mh_volume *v, float lambda, int iterations, void *stream);
  * come out as -inf.  The nine scratch planes live in one fixed device array of
  * MH_TV_STATIC_MAX_PIXELS * 9 floats (about 11 MB), held by every GPU that
  * loads the library until the process exits; images with more than
- * MH_TV_STATIC_MAX_PIXELS pixels are rejected with MH_ERR_CAPACITY.  The
- * first call on a device looks up the array's device address (once per
- * device, with that device current); make that first call before any stream
- * capture.  All calls share the array: each call initialises every plane it
+ * MH_TV_STATIC_MAX_PIXELS pixels are rejected with MH_ERR_CAPACITY.  Each
+ * call made while `stream` is not capturing looks up the array's device
+ * address with the current device (a lookup, not an allocation), so a
+ * cudaDeviceReset, after which the array may move, is followed; a call made
+ * while the stream captures reuses the address the last such lookup found on
+ * that device, so make one call on each device before any stream capture.
+ * All calls share the array: each call initialises every plane it
  * reads, and calls that overlap on the GPU (other streams, other threads) race
  * on it.  Nothing is allocated or freed, on the device or the host. */
 #define MH_TV_STATIC_MAX_PIXELS (640 * 480)

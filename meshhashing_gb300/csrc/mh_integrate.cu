@@ -329,11 +329,13 @@ __global__ void __launch_bounds__(256) k_vtx_select_b(const Scene *t, int n) {
 }
 
 // Sensor::Process tail: depth validity (ConvertDepthFormatKernel,
-// sensor/preprocess.cu:25-42) and inlier-ratio reset to 0.1 (:10-23).
+// sensor/preprocess.cu:25-42) and inlier-ratio reset to 0.1 (:10-23).  Raw
+// 16-bit depth is read as the reference reads it, through a signed short, so
+// raw values of 32768 and above are negative depths and invalid.
 __device__ __forceinline__ void preprocess_body(const Dev &d, const float *src, const uint16_t *src16, float range_factor) {
   const int n = d.p.width * d.p.height;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float z = src16 ? range_factor * (float)src16[i] : src[i];
+    float z = src16 ? range_factor * (float)(int16_t)src16[i] : src[i];
     const bool ok = z >= d.p.min_depth_range && z <= d.p.max_depth_range;
     d.depth[i] = ok ? z : -__int_as_float(0x7f800000);
     d.inlier[i] = 0.1f;

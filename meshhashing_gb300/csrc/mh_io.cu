@@ -7,9 +7,12 @@
 //           4: also the PSDF a and b), f32 voxel size, f32 truncation
 //           distance, f32 truncation scale
 //   blocks  per block: i32 x, y, z, then 512 floats per field
-// Save and load stream the blocks in chunks, so the host holds at most one
-// chunk.  Loading inserts the blocks into the hash (the same path as
-// mh_load_blocks) and leaves the mesh to the next mesh pass.
+// Save and load stream the blocks in chunks of at most kIoChunk blocks (the
+// host buffers hold one chunk of the file's fields, 16 MB at 4 fields), so a
+// small map needs small buffers.  Loading inserts the blocks into the hash
+// (the same path as mh_load_blocks) and leaves the mesh to the next mesh
+// pass.  A file whose field count, voxel size or truncation differs from the
+// volume's is refused before anything is inserted.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -23,7 +26,7 @@ extern "C" int mh_load_blocks(mh_volume *v, int n, const int32_t *pos, const flo
 
 namespace {
 const char kMagic[8] = {'M', 'H', 'V', 'O', 'L', '0', '1', '\0'};
-constexpr int kIoChunk = 1 << 16;
+constexpr int kIoChunk = 1 << 11;
 struct Header {
   char magic[8];
   uint32_t blocks, fields;
@@ -50,17 +53,18 @@ int mh_save_volume(mh_volume *v, const char *path) {
   h.voxel_size = v->hp.voxel_size, h.truncation = v->hp.truncation_distance;
   h.truncation_scale = v->hp.truncation_distance_scale;
   bool ok = fwrite(&h, sizeof(h), 1, f) == 1;
-  std::vector<int4> bp(kIoChunk);
-  std::vector<float> rows((size_t)kIoChunk * MH_BLOCK_VOXELS * nf);
+  const int chunk = std::max(1, std::min(kIoChunk, hw));
+  std::vector<int4> bp(chunk);
+  std::vector<float> rows((size_t)chunk * MH_BLOCK_VOXELS * nf);
   uint32_t written = 0;
-  for (int base = 0; base < hw && ok; base += kIoChunk) {
-    const int n = std::min(kIoChunk, hw - base);
+  for (int base = 0; base < hw && ok; base += chunk) {
+    const int n = std::min(chunk, hw - base);
     if (cudaMemcpy(bp.data(), v->d.block_pos + base, sizeof(int4) * n, cudaMemcpyDeviceToHost) != cudaSuccess) {
       ok = false;
       break;
     }
     for (int fi = 0; fi < nf && ok; ++fi)
-      ok = cudaMemcpy(rows.data() + (size_t)fi * kIoChunk * MH_BLOCK_VOXELS,
+      ok = cudaMemcpy(rows.data() + (size_t)fi * chunk * MH_BLOCK_VOXELS,
                       fields[fi] + (size_t)base * MH_BLOCK_VOXELS, sizeof(float) * MH_BLOCK_VOXELS * n,
                       cudaMemcpyDeviceToHost) == cudaSuccess;
     for (int i = 0; i < n && ok; ++i) {
@@ -68,7 +72,7 @@ int mh_save_volume(mh_volume *v, const char *path) {
       const int32_t p3[3] = {bp[i].x, bp[i].y, bp[i].z};
       ok = fwrite(p3, sizeof(int32_t), 3, f) == 3;
       for (int fi = 0; fi < nf && ok; ++fi)
-        ok = fwrite(rows.data() + ((size_t)fi * kIoChunk + i) * MH_BLOCK_VOXELS, sizeof(float), MH_BLOCK_VOXELS,
+        ok = fwrite(rows.data() + ((size_t)fi * chunk + i) * MH_BLOCK_VOXELS, sizeof(float), MH_BLOCK_VOXELS,
                     f) == MH_BLOCK_VOXELS;
       ++written;
     }
@@ -86,32 +90,38 @@ int mh_load_volume(mh_volume *v, const char *path, int *n_blocks) {
   FILE *f = fopen(path, "rb");
   if (!f) return MH_ERR_INVALID;
   Header h;
-  if (fread(&h, sizeof(h), 1, f) != 1 || memcmp(h.magic, kMagic, 8) != 0 || (h.fields != 2 && h.fields != 4) ||
-      h.voxel_size != v->hp.voxel_size) {
+  // the file must hold the fields this volume's update keeps (2: sdf and
+  // weight of the simple update, 4: also the PSDF a and b) and come from the
+  // same voxel size and truncation
+  const uint32_t want_fields = v->hp.enable_bayesian_update ? 4u : 2u;
+  if (fread(&h, sizeof(h), 1, f) != 1 || memcmp(h.magic, kMagic, 8) != 0 || h.fields != want_fields ||
+      h.voxel_size != v->hp.voxel_size || h.truncation != v->hp.truncation_distance ||
+      h.truncation_scale != v->hp.truncation_distance_scale) {
     fclose(f);
     return MH_ERR_INVALID;
   }
   const int nf = (int)h.fields;
-  std::vector<int32_t> pos((size_t)kIoChunk * 3);
-  std::vector<float> fld((size_t)kIoChunk * MH_BLOCK_VOXELS * 4, 0.0f);
+  const int chunk = (int)std::max<uint32_t>(1, std::min<uint32_t>(kIoChunk, h.blocks));
+  std::vector<int32_t> pos((size_t)chunk * 3);
+  std::vector<float> fld((size_t)chunk * MH_BLOCK_VOXELS * nf, 0.0f);
   std::vector<float> rec((size_t)MH_BLOCK_VOXELS * nf);
   int r = MH_OK;
   uint32_t done = 0;
   while (done < h.blocks && r == MH_OK) {
-    const int n = (int)std::min<uint32_t>(kIoChunk, h.blocks - done);
+    const int n = (int)std::min<uint32_t>(chunk, h.blocks - done);
     for (int i = 0; i < n && r == MH_OK; ++i) {
       if (fread(&pos[3 * i], sizeof(int32_t), 3, f) != 3 || fread(rec.data(), sizeof(float), rec.size(), f) != rec.size()) {
         r = MH_ERR_INVALID;
         break;
       }
       for (int fi = 0; fi < nf; ++fi)
-        memcpy(&fld[((size_t)fi * kIoChunk + i) * MH_BLOCK_VOXELS], &rec[(size_t)fi * MH_BLOCK_VOXELS],
+        memcpy(&fld[((size_t)fi * chunk + i) * MH_BLOCK_VOXELS], &rec[(size_t)fi * MH_BLOCK_VOXELS],
                sizeof(float) * MH_BLOCK_VOXELS);
     }
     if (r != MH_OK) break;
-    const float *F[4] = {fld.data(), fld.data() + (size_t)kIoChunk * MH_BLOCK_VOXELS,
-                         nf == 4 ? fld.data() + (size_t)2 * kIoChunk * MH_BLOCK_VOXELS : nullptr,
-                         nf == 4 ? fld.data() + (size_t)3 * kIoChunk * MH_BLOCK_VOXELS : nullptr};
+    const float *F[4] = {fld.data(), fld.data() + (size_t)chunk * MH_BLOCK_VOXELS,
+                         nf == 4 ? fld.data() + (size_t)2 * chunk * MH_BLOCK_VOXELS : nullptr,
+                         nf == 4 ? fld.data() + (size_t)3 * chunk * MH_BLOCK_VOXELS : nullptr};
     r = mh_load_blocks(v, n, pos.data(), F[0], F[1], F[2], F[3]);
     done += (uint32_t)n;
   }

@@ -307,19 +307,26 @@ extern "C" int mh_denoise_tv_static(const float *depth_in, float *depth_out, int
   if ((long long)width * height > (long long)MH_TV_STATIC_MAX_PIXELS) return MH_ERR_CAPACITY;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MH_ERR_CUDA;
+  cudaStream_t s = (cudaStream_t)stream;
   float *scratch = nullptr;
   {
-    // first call on a device: resolve the device address of the array (host
-    // code only sees a host-side stand-in for it)
+    // Host code only sees a host-side stand-in for the array, so its device
+    // address is looked up with the device current.  Outside a stream
+    // capture the lookup runs on every call: after cudaDeviceReset the
+    // module is loaded again and the array may sit at another address.
+    // While the stream captures, the address found by the last call outside
+    // a capture on this device is used.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return MH_ERR_CUDA;
     std::lock_guard<std::mutex> lock(g_tv_static_mu);
-    if (!g_tv_static_ptr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone) {
       void *p = nullptr;
       if (cudaGetSymbolAddress(&p, g_tv_static_scratch) != cudaSuccess || !p) return MH_ERR_CUDA;
       g_tv_static_ptr[dev] = static_cast<float *>(p);
     }
     scratch = g_tv_static_ptr[dev];
+    if (!scratch) return MH_ERR_INVALID;
   }
-  cudaStream_t s = (cudaStream_t)stream;
   const int n = width * height;
   const int g = min((n + 255) / 256, mh_sm_count() * 8);
   float *f = scratch;

@@ -43,12 +43,20 @@ struct StageScope {
   }
 };
 
+// SM count of the current device, cached per device ordinal (threads may
+// race to fill an entry; they all store the same value)
 int mh_sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = 0;
+  if (dev >= 64) {
+    int n = 0;
+    return cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0 ? n : 132;
+  }
+  int n = cache[dev].load(std::memory_order_relaxed);
+  if (n <= 0) {
     if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 132;
+    cache[dev].store(n, std::memory_order_relaxed);
   }
   return n;
 }
@@ -640,6 +648,10 @@ int mh_load_blocks(mh_volume *v, int n, const int32_t *pos, const float *sdf, co
   CHECK_VOL(v);
   if (n < 0 || (n > 0 && !pos)) return MH_ERR_INVALID;
   MH_CUDA_TRY(cudaDeviceSynchronize());
+  // Every position is inserted before any voxel data moves.  On
+  // MH_ERR_CAPACITY the blocks that did fit stay allocated with the voxel
+  // values they held before (zero for new blocks): the caller may free them
+  // with mh_gc_* or reset the volume.
   std::vector<int> ptr;
   TRY(find_ptrs(v, n, pos, ptr, true));
   for (int i = 0; i < n; ++i)
@@ -650,16 +662,21 @@ int mh_load_blocks(mh_volume *v, int n, const int32_t *pos, const float *sdf, co
   int *dptr = reinterpret_cast<int *>(buf + nv * 4);
   const float *srcs[4] = {sdf, weight, a, b};
   float *dsts[4] = {nullptr, nullptr, nullptr, nullptr};
-  for (int f = 0; f < 4; ++f) {
+  cudaError_t e = cudaSuccess;
+  for (int f = 0; f < 4 && e == cudaSuccess; ++f) {
     if (!srcs[f]) continue;
     dsts[f] = buf + nv * f;
-    cudaMemcpy(dsts[f], srcs[f], sizeof(float) * nv, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(dsts[f], srcs[f], sizeof(float) * nv, cudaMemcpyHostToDevice);
   }
-  cudaMemcpy(dptr, ptr.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
-  if (n > 0) k_scatter_fields<<<n, 128>>>(v->d, dptr, n, dsts[0], dsts[1], dsts[2], dsts[3]);
-  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(dptr, ptr.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+  // a failed upload scatters nothing
+  if (e == cudaSuccess && n > 0) {
+    k_scatter_fields<<<n, 128>>>(v->d, dptr, n, dsts[0], dsts[1], dsts[2], dsts[3]);
+    e = cudaGetLastError();
+  }
+  const cudaError_t es = cudaDeviceSynchronize();
   cudaFree(buf);
-  return e == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+  return e == cudaSuccess && es == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }
 
 int mh_dump_candidates(mh_volume *v, int max_n, int32_t *pos, int *n_out) {

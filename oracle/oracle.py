@@ -119,6 +119,16 @@ def inverse(m):
     return out.reshape(4, 4)
 
 
+def convert_depth_u16(raw, range_factor, min_depth, max_depth):
+    """ConvertDepthFormatKernel (sensor/preprocess.cu:25-42) in numpy: the raw
+    image is a short*, depth = range_factor * src in single precision, valid
+    inside [min, max], else -inf."""
+    src = np.asarray(raw).astype(np.uint16).view(np.int16).astype(np.float32)
+    z = np.float32(range_factor) * src
+    ok = (z >= np.float32(min_depth)) & (z <= np.float32(max_depth))
+    return np.where(ok, z, np.float32(-np.inf)).astype(np.float32)
+
+
 def set_threads(n):
     lib().orc_set_threads(int(n))
 

@@ -21,9 +21,22 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT_DIR, "librefcpu.so")
+# where the reference tree is read from: MESHHASHING_REFERENCE, else the
+# read-only mount this recipe was written for
+DEFAULT_REF = "/root/reference"
 
 
-def build(ref_root: str = "/root/reference", force: bool = False) -> str:
+def reference_dir() -> str:
+    """The reference source tree (``$MESHHASHING_REFERENCE`` overrides)."""
+    return os.environ.get("MESHHASHING_REFERENCE", DEFAULT_REF)
+
+
+def have_reference() -> bool:
+    return os.path.isdir(os.path.join(reference_dir(), "src"))
+
+
+def build(ref_root: str = None, force: bool = False) -> str:
+    ref_root = ref_root or reference_dir()
     src = os.path.join(HERE, "refcpu", "refcpu.cpp")
     deps = [src, os.path.join(HERE, "refcpu", "cuda_host.h"), os.path.join(HERE, "refcpu", "extract.py")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):

@@ -4,7 +4,8 @@ The reference has no tests or golden vectors, so its own device code, built
 for the CPU (oracle/refcpu: the reference's kernels and headers compiled with
 g++ against a CUDA-emulation shim), is run on small seeded inputs through
 the MainEngine stage order, and its outputs are stored together with the
-inputs.  Needs the reference tree (default /root/reference); the fixtures are
+inputs.  Needs the reference tree (argument 1, else $MESHHASHING_REFERENCE,
+else oracle/refcpu.py's default); the fixtures are
 committed, so tests never need the tree.
 
   simple_room96.npz  plain TSDF chain, 96x72, 8 mm voxels, 6 frames of the
@@ -192,8 +193,8 @@ def rows(pos, field, want):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     from oracle import refcpu
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else refcpu.reference_dir()
     refcpu.build(ref_root)
     p, depth, poses = simple_case()
     np.savez_compressed(os.path.join(HERE, "simple_room96.npz"), **run_simple(refcpu, p, depth, poses))

@@ -13,7 +13,9 @@ from meshhashing_gb300 import config, scene
 from oracle import oracle as O
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+from oracle.refcpu import reference_dir
+
+REF = reference_dir()
 
 
 def teschner(x, y, z, n):

@@ -14,6 +14,11 @@ import pytest
 from tests import _golden
 
 
+def _have_reference():
+    from oracle.refcpu import have_reference
+    return have_reference()
+
+
 def test_oracle_matches_reference_simple_chain(built):
     ntri, other_end = _golden.check_simple(_golden.OracleRunner)
     assert ntri > 500
@@ -51,7 +56,7 @@ def test_oracle_matches_reference_huber_tv(built):
     np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference"), reason="reference sources not present")
+@pytest.mark.skipif(not _have_reference(), reason="reference sources not present")
 def test_fixtures_regenerate_from_reference(built, tmp_path):
     """The committed fixtures are what the reference's code produces now."""
     import numpy as np

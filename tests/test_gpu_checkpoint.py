@@ -55,3 +55,33 @@ def test_save_load_round_trip(built, tmp_path, psdf):
     assert np.array_equal(pa, pb)
     np.testing.assert_array_equal(fa["sdf"].view(np.uint32), fb["sdf"].view(np.uint32))
     assert a.stats()["error"] == 0 and b.stats()["error"] == 0
+
+
+def test_load_refuses_mismatched_file(built, tmp_path):
+    """A checkpoint whose update mode (field count), voxel size or truncation
+    differs from the volume's is refused before any block is inserted."""
+    from meshhashing_gb300 import MeshHashError
+    wl = scene.full_spline(4, width=128, height=96)
+    kw = dict(value_capacity=1 << 14, bucket_count=1 << 14, max_vertex_count=1 << 16, max_triangle_count=1 << 16)
+    p = config.params_for(wl, **kw)
+    a = Volume(p)
+    for i in range(2):
+        a.integrate_frame(wl.frame(i), wl.pose(i))
+    path = tmp_path / "psdf.mhvol"
+    a.save(path)
+    others = [config.params_for(wl, bayesian=False, **kw),                 # 2-field volume, 4-field file
+              config.params_for(wl, voxel_size=0.005, **kw),
+              config.params_for(wl, truncation=0.016, **kw)]
+    for q in others:
+        b = Volume(q)
+        with pytest.raises(MeshHashError):
+            b.load(path)
+        assert b.stats()["blocks_allocated"] == 0
+    # and the other way round: a 2-field file into a PSDF volume
+    s = Volume(config.params_for(wl, bayesian=False, **kw))
+    s.integrate_frame(wl.frame(0), wl.pose(0))
+    s.save(tmp_path / "simple.mhvol")
+    b = Volume(p)
+    with pytest.raises(MeshHashError):
+        b.load(tmp_path / "simple.mhvol")
+    assert b.stats()["blocks_allocated"] == 0
