@@ -9,6 +9,7 @@
 // only loaded when at least one of the thread's voxels projects onto a valid
 // depth pixel inside the truncation band.
 #include "mh_internal.cuh"
+#include "mh_exp.h"
 #include "mh_kernels.h"
 #include "mh_batch.cuh"
 
@@ -209,7 +210,7 @@ __device__ __forceinline__ void integrate_psdf_body(const Dev &d) {
       const float isv = 1.0f / sv;
       const float dx = x - mu;
       // gaussian(): exp(-dx^2 / sv) / sqrt(2 pi sv)
-      const float g = expf(-(dx * dx) * isv) * (sqrtf(sv) * isv) * 0.398942280401432678f;
+      const float g = mh_expf(-(dx * dx) * isv) * (sqrtf(sv) * isv) * 0.398942280401432678f;
       float C1 = r * g;
       float C2 = in_range ? (1.0f - r) * 0.204081632653061224f : 1.0f;
       const float isum = 1.0f / (C1 + C2);
@@ -288,8 +289,11 @@ __device__ __forceinline__ void predict_inlier_body(const Dev &d) {
         const float pd = dot3(vec, cn);
         const float disk = sqrtf(dot3(vec, vec) - pd * pd);
         const float q = pd - vsdf;
-        const float w_dist = expf(-(q * q) * vw);
-        const float w_disk = 0.5f + 0.5f / (1.0f + expf(-fabsf(disk / vt.radius)));
+        // the library's own exp (mh_exp.h) unless the reference's arithmetic
+        // is asked for
+        const float e_dist = -(q * q) * vw, e_disk = -fabsf(disk / vt.radius);
+        const float w_dist = p.compat ? expf(e_dist) : mh_expf(e_dist);
+        const float w_disk = 0.5f + 0.5f / (1.0f + (p.compat ? expf(e_disk) : mh_expf(e_disk)));
         float w_ang = (cos_a - 0.1736f) / (1.0f - 0.1736f);
         w_ang = fmaxf(w_ang, 0.1f);
         float ir = w_disk * w_dist * w_ang;

@@ -46,6 +46,7 @@
 #endif
 
 #include "../include/meshhash.h"
+#include "../meshhashing_gb300/csrc/mh_exp.h"
 
 namespace orc {
 
@@ -345,6 +346,10 @@ template <class R> struct Vol {
   // double): forward differences over valid pixel pairs, tau = sigma =
   // 1/sqrt(8), theta = 1, invalid pixels stay invalid.
   void denoise_tv(double lambda, int iters) {
+    if (sizeof(R) == 4) {
+      denoise_tv_f32((float)lambda, iters);
+      return;
+    }
     const int W = p.width, H = p.height;
     const size_t n = (size_t)W * H;
     std::vector<double> f(n, 0), u(n), ub(n), px(n, 0), py(n, 0), u2(n), ub2(n), px2(n), py2(n);
@@ -388,6 +393,58 @@ template <class R> struct Vol {
       u.swap(u2), ub.swap(ub2), px.swap(px2), py.swap(py2);
     }
     for (size_t i = 0; i < n; ++i) depth[i] = ok[i] ? (float)(u[i] * 0.001) : -INFINITY;
+  }
+
+  // The same iteration in single precision, in the operation order of the
+  // library's kernels (every value a correctly rounded +, -, *, /, sqrt or
+  // max of the previous iterate), so its output is bit-identical to theirs:
+  // depth in millimetres z * 1000, tau = sigma = 1/sqrt(8) rounded to float,
+  // u' = (u + tau div + (tau lambda) f) / (1 + tau lambda), output u' * 0.001.
+  void denoise_tv_f32(float lambda, int iters) {
+    const int W = p.width, H = p.height;
+    const size_t n = (size_t)W * H;
+    std::vector<float> f(n), u(n), ub(n), px(n, 0.0f), py(n, 0.0f), u2(n), ub2(n), px2(n), py2(n);
+    std::vector<uint8_t> ok(n);
+    for (size_t i = 0; i < n; ++i) {
+      const float z = depth[i];
+      ok[i] = z > 0.0f && z < 1e30f;
+      f[i] = ok[i] ? z * 1000.0f : -INFINITY;
+      u[i] = ub[i] = f[i];
+    }
+    const float tau = 0.35355339059327373f, sigma = 0.35355339059327373f;
+    auto dual = [&](int x, int y, float &ox, float &oy) {
+      const size_t i = (size_t)y * W + x;
+      float gx = 0.0f, gy = 0.0f;
+      if (ok[i] && x + 1 < W && ok[i + 1]) gx = ub[i + 1] - ub[i];
+      if (ok[i] && y + 1 < H && ok[i + W]) gy = ub[i + W] - ub[i];
+      const float qx = px[i] + sigma * gx, qy = py[i] + sigma * gy;
+      const float nr = std::fmax(1.0f, std::sqrt(qx * qx + qy * qy));
+      ox = qx / nr, oy = qy / nr;
+    };
+    for (int it = 0; it < iters; ++it) {
+#pragma omp parallel for schedule(static)
+      for (int y = 0; y < H; ++y) {
+        for (int x = 0; x < W; ++x) {
+          const size_t i = (size_t)y * W + x;
+          float pxc, pyc, pxl = 0.0f, pyu = 0.0f, dm;
+          dual(x, y, pxc, pyc);
+          px2[i] = pxc, py2[i] = pyc;
+          if (!ok[i]) {
+            u2[i] = ub2[i] = f[i];
+            continue;
+          }
+          if (x > 0) dual(x - 1, y, pxl, dm);
+          if (y > 0) dual(x, y - 1, dm, pyu);
+          const float div = (pxc - pxl) + (pyc - pyu);
+          const float u0 = u[i];
+          const float un = (u0 + tau * div + tau * lambda * f[i]) / (1.0f + tau * lambda);
+          u2[i] = un;
+          ub2[i] = 2.0f * un - u0;
+        }
+      }
+      u.swap(u2), ub.swap(ub2), px.swap(px2), py.swap(py2);
+    }
+    for (size_t i = 0; i < n; ++i) depth[i] = ok[i] ? u[i] * 0.001f : -INFINITY;
   }
 
   bool depth_invalid(float d) const {
@@ -550,6 +607,13 @@ template <class R> struct Vol {
   }
 
   // ---------------------------------------------------------- PSDF
+  // exp of the single-precision path: the library's exp (mh_exp.h, basic IEEE
+  // operations only, so bit-identical on the GPU and here); the reference's
+  // arithmetic (compat) and the FP64 oracle use the C library's
+  R ex(R v) const {
+    if (sizeof(R) == 4 && !p.compat_arithmetic) return (R)mh_expf((float)v);
+    return std::exp(v);
+  }
   static R gaussian(R x, R u, R s2) {
     // geometry/geometry_helper.h:30-34 (no 1/2 in the exponent)
     R c = sizeof(R) == 8 ? (R)std::sqrt(2 * M_PI) : (R)2.50662827463100050f;
@@ -590,8 +654,8 @@ template <class R> struct Vol {
           R pd = dot(vec, cn);
           R disk = std::sqrt(dot(vec, vec) - pd * pd);
           R q = pd - b->sdf[i];
-          R w_dist = std::exp(-(q * q) * b->w[i]);
-          R w_disk = (R)0.5 + (R)0.5 / ((R)1 + std::exp(-std::fabs(disk / r)));
+          R w_dist = ex(-(q * q) * b->w[i]);
+          R w_disk = (R)0.5 + (R)0.5 / ((R)1 + ex(-std::fabs(disk / r)));
           R w_ang = (cos_a - (R)0.1736f) / ((R)1 - (R)0.1736f);
           w_ang = std::fmax(w_ang, (R)0.1f);
           R ir = w_disk * w_dist * w_ang;
@@ -653,7 +717,7 @@ template <class R> struct Vol {
           const float sv = s2 + t2f;
           const float isv = 1.0f / sv;
           const float dx = xf - muf;
-          const float g = std::exp(-(dx * dx) * isv) * (std::sqrt(sv) * isv) * 0.398942280401432678f;
+          const float g = mh_expf(-(dx * dx) * isv) * (std::sqrt(sv) * isv) * 0.398942280401432678f;
           float C1 = rf * g;
           float C2 = in_range ? (1.0f - rf) * 0.204081632653061224f : 1.0f;
           const float isum = 1.0f / (C1 + C2);
@@ -2017,6 +2081,16 @@ void orc_huber_iterate(void *hp, float lambda, float sigma, float tau, int iters
   });
 }
 
+// the single-precision exp of the PSDF path (mh_exp.h), for its accuracy test
+void orc_expf(int n, const float *x, float *out) {
+  for (int i = 0; i < n; ++i) out[i] = mh_expf(x[i]);
+}
+// replace the current frame's preprocessed depth (after orc_frame_set), e.g.
+// with the library's denoised frame, so later stages start from the same input
+void orc_set_depth(void *hp, const float *d) {
+  OHandle *h = (OHandle *)hp;
+  DISPATCH(h, std::copy(d, d + vol->depth.size(), vol->depth.begin()));
+}
 void orc_denoise_tv(void *hp, float lambda, int iters) {
   OHandle *h = (OHandle *)hp;
   DISPATCH(h, vol->denoise_tv(lambda, iters));

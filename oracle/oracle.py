@@ -21,6 +21,7 @@ SRC = os.path.join(HERE, "mh_oracle.cpp")
 def build(force: bool = False) -> str:
     """Compile liboracle.so with g++ (OpenMP, no FMA contraction)."""
     deps = [SRC, os.path.join(HERE, "..", "meshhashing_gb300", "csrc", "mc_cases.inc"),
+            os.path.join(HERE, "..", "meshhashing_gb300", "csrc", "mh_exp.h"),
             os.path.join(HERE, "..", "include", "meshhash.h")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
@@ -79,6 +80,8 @@ def lib():
         L.orc_frame.argtypes = [vp, f32p, f32p, C.c_int, C.c_float, f32p, f32p, f32p]
         L.orc_denoise_tv.argtypes = [vp, C.c_float, C.c_int]
         L.orc_get_depth.argtypes = [vp, f32p]
+        L.orc_set_depth.argtypes = [vp, f32p]
+        L.orc_expf.argtypes = [C.c_int, f32p, f32p]
         L.orc_huber_init.argtypes = [vp]
         L.orc_point_to_psdf.argtypes = [vp, f32p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                         C.POINTER(C.c_double), i32p]
@@ -117,6 +120,14 @@ def inverse(m):
     out = np.zeros(16, np.float32)
     lib().orc_inverse(_p(m, C.c_float), _p(out, C.c_float))
     return out.reshape(4, 4)
+
+
+def expf(x):
+    """The library's single-precision exp (mh_exp.h) evaluated on the CPU."""
+    x = f32(x).reshape(-1)
+    out = np.empty_like(x)
+    lib().orc_expf(x.size, _p(x, C.c_float), _p(out, C.c_float))
+    return out
 
 
 def convert_depth_u16(raw, range_factor, min_depth, max_depth):
@@ -299,6 +310,12 @@ class Oracle:
         out = np.zeros(self.W * self.H, np.float32)
         self.L.orc_get_depth(self.h, _p(out, C.c_float))
         return out.reshape(self.H, self.W)
+
+    def set_depth(self, img):
+        """Replace the current frame's preprocessed depth (after frame_set)."""
+        a = f32(img).reshape(-1)
+        assert a.size == self.W * self.H
+        self.L.orc_set_depth(self.h, _p(a, C.c_float))
 
     # ---- state exchange
     def block_count(self):

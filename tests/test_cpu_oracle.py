@@ -221,3 +221,22 @@ def test_oracle_mesh_lies_on_surfaces(built):
     # reference counts equal the number of triangle uses
     uses = np.bincount(tr[:, 4:7].ravel(), minlength=len(vk))
     np.testing.assert_array_equal(uses, vd[:, 7].astype(np.int64))
+
+
+def test_library_exp_within_one_ulp(built):
+    """mh_exp.h (the single-precision exp of the PSDF path, shared by the
+    kernels and the FP32 oracle) against double-precision exp rounded to
+    single: at most 1 ulp on 2 M log-spaced and random arguments, exact at
+    0, and the overflow / underflow ends."""
+    rng = np.random.default_rng(3)
+    x = np.concatenate([rng.uniform(-103.9, 88.7, 1 << 20),
+                        -np.logspace(-8, np.log10(103.9), 1 << 19), np.logspace(-8, np.log10(88.7), 1 << 19),
+                        [0.0, -0.0, 88.72, -87.33, -103.0, -103.97]]).astype(np.float32)
+    got = O.expf(x)
+    want = np.exp(x.astype(np.float64)).astype(np.float32)
+    gi, wi = got.view(np.int32).astype(np.int64), want.view(np.int32).astype(np.int64)
+    assert np.abs(gi - wi).max() <= 1
+    assert O.expf(np.array([0.0], np.float32))[0] == 1.0
+    assert np.isinf(O.expf(np.array([89.0], np.float32))[0])
+    assert O.expf(np.array([-104.0], np.float32))[0] == 0.0
+    assert np.isnan(O.expf(np.array([np.nan], np.float32))[0])

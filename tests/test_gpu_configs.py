@@ -1,0 +1,294 @@
+"""Parity at the workloads' own configurations, not at reduced sizes.
+
+* C1, as stated: 320x240, fx = fy = 262.5, 60 frames of the circle, 8 mm
+  voxels, truncation 3 voxels, 2^18 x 4 hash, simple update (weight_sample
+  200, so the MC weight gate 1/voxel^2 is reached).  The library's frame
+  chain (mh_integrate_frame) and the FP32 oracle's MainEngine loop run side by
+  side from an empty volume: block sets, voxel bits, mesh topology and
+  raycast bits must be identical; the last frame is then checked stage by
+  stage against the FP64 oracle.
+* C2's shape: 640x480, fx = fy = 525, 4 mm voxels, truncation 12 mm, 2^21
+  buckets, the benchmark's pool sizes, TV lambda = 0.1 x 20 iterations, PSDF
+  update.  First five whole frames from an empty volume, side by side with the
+  FP32 oracle (the library's exp and the single-precision TV are restated
+  bit for bit, so every value must match); then one frame stage by stage on a
+  20-frame map, each stage started from the GPU's own state, against the FP32
+  oracle (bits) and the FP64 oracle (bounds, max errors printed).
+
+Reference functions: mapping/allocate.cu:8-99, core/collect_block_array.cu:25-59,
+mapping/update_simple.cu:13-77, mapping/update_bayesian.cu:16-185,
+meshing/marching_cubes.cu:326-382, visualization/ray_caster.cu:16-150.
+"""
+import numpy as np
+import pytest
+
+from meshhashing_gb300 import Volume, config, scene
+from oracle.oracle import Oracle
+from tests._util import mesh_canon, tri_counts_per_block
+
+pytestmark = pytest.mark.gpu
+
+
+def keys(pos):
+    p = np.asarray(pos, np.int64).reshape(-1, 3) + (1 << 20)
+    return (p[:, 0] << 42) | (p[:, 1] << 21) | p[:, 2]
+
+
+def same_set(a, b):
+    ka, kb = np.sort(keys(a)), np.sort(keys(b))
+    return ka.shape == kb.shape and np.array_equal(ka, kb)
+
+
+def aligned(gpos, gfield, opos, ofield):
+    """Rows of both fields for the blocks present in both, in one order."""
+    _, gi, oi = np.intersect1d(keys(gpos), keys(opos), assume_unique=True, return_indices=True)
+    return gfield[gi], ofield[oi]
+
+
+def bits_equal(a, b):
+    return np.array_equal(np.ascontiguousarray(a, np.float32).view(np.uint32),
+                          np.ascontiguousarray(b, np.float32).view(np.uint32))
+
+
+def hand_over(v, o, with_mesh=False):
+    pos, f = v.dump_blocks()
+    o.set_blocks(pos, f["sdf"], f["w"], f["a"], f["b"])
+    if with_mesh:
+        vk, vd, tr = v.dump_mesh()
+        o.load_mesh(vk, vd, tr)
+        o.set_cubes(pos, v.cubes(pos))
+        life, inner, bnd = v.block_meta(pos)
+        o.set_block_meta(pos, life, inner, bnd)
+    return pos, f
+
+
+def compare_volumes(v, o, fields, what):
+    gpos, gf = v.dump_blocks(fields)
+    opos, os_, ow, oa, ob = o.blocks()
+    assert same_set(gpos, opos), f"{what}: block sets differ ({len(gpos)} vs {len(opos)})"
+    ofield = {"sdf": os_, "w": ow, "a": oa, "b": ob}
+    for k in fields:
+        g, oo = aligned(gpos, gf[k], opos, ofield[k])
+        assert bits_equal(g, oo), f"{what}: {k} differs in {int((g != oo).sum())} voxels"
+    return len(gpos)
+
+
+def compare_mesh(v, o, what):
+    gverts, gtris = mesh_canon(*v.dump_mesh())
+    overts, otris = mesh_canon(*o.dump_mesh())
+    assert set(gverts) == set(overts), f"{what}: vertex sets differ"
+    assert gtris == otris, f"{what}: triangle topology differs"
+    assert tri_counts_per_block(gtris) == tri_counts_per_block(otris)
+    keys_ = sorted(gverts)
+    gp = np.stack([gverts[k] for k in keys_]) if keys_ else np.zeros((0, 8), np.float32)
+    op = np.stack([overts[k] for k in keys_]) if keys_ else np.zeros((0, 8), np.float32)
+    np.testing.assert_array_equal(gp[:, 7], op[:, 7])      # reference counts
+    return len(keys_), len(gtris), gp, op
+
+
+# ---------------------------------------------------------------------- C1
+def c1():
+    wl = scene.small_circle(60)
+    assert (wl.camera.width, wl.camera.height, wl.camera.fx, wl.camera.fy) == (320, 240, 262.5, 262.5)
+    p = config.params_for(wl)
+    assert (p.voxel_size, p.truncation_distance, p.bucket_count, p.bucket_size, p.enable_bayesian_update) == \
+        (np.float32(0.008), np.float32(0.024), 1 << 18, 4, 0)
+    return wl, p
+
+
+def test_c1_whole_chain_exact(built):
+    wl, p = c1()
+    v = Volume(p)
+    o = Oracle(p, fp64=False)
+    W, H = p.rc_width, p.rc_height
+    gd = np.empty((H, W), np.float32)
+    for i in range(60):
+        d, T = wl.frame(i), wl.pose(i)
+        v.integrate_frame(d, T, ray_depth=gd)
+        od = o.frame(d, T, raycast=True)
+        if i % 10 == 9 or i == 59:
+            nb = compare_volumes(v, o, ("sdf", "w"), f"C1 frame {i}")
+            nv, nt, gp, op = compare_mesh(v, o, f"C1 frame {i}")
+            pos_err = float(np.abs(gp[:, :3] - op[:, :3]).max()) / p.voxel_size if nv else 0.0
+            assert pos_err < 1e-4, (i, pos_err)
+            assert np.array_equal(np.isfinite(gd), np.isfinite(od)), f"C1 frame {i}: raycast hit masks differ"
+            assert bits_equal(gd[np.isfinite(gd)], od[np.isfinite(od)]), f"C1 frame {i}: raycast depth differs"
+    st = v.stats()
+    assert st["error"] == 0 and st["dropped_inserts"] == 0
+    assert nt > 0, "C1 meshes nothing: the MC weight gate was not reached"
+    print(f"C1 60 frames: {nb} blocks, {nv} vertices, {nt} triangles, {int(np.isfinite(gd).sum())} ray hits, "
+          f"identical to the FP32 oracle (vertex positions within {pos_err:.1e} voxel)")
+
+    # one more frame stage by stage against FP64
+    o64 = Oracle(p, fp64=True)
+    d, T = wl.frame(59), wl.pose(59)
+    v.set_frame(d, T)
+    v.alloc_block_array()
+    v.collect_blocks_in_frustum()
+    cand = v.candidates()
+    pos, f = hand_over(v, o64, with_mesh=True)
+    o64.frame_set(d, T)
+    o64.set_candidates(cand)
+    v.update_blocks_simple()
+    o64.integrate_simple()
+    gpos, gf = v.dump_blocks(("sdf", "w"))
+    p64, s64, w64, _, _ = o64.blocks()
+    gs, os6 = aligned(gpos, gf["sdf"], p64, s64)
+    gw, ow6 = aligned(gpos, gf["w"], p64, w64)
+    m = ow6 > 0
+    e_sdf = float(np.abs(gs - os6)[m].max())
+    e_w = float((np.abs(gw - ow6)[m] / ow6[m]).max())
+    v.marching_cubes()
+    o64.mesh()
+    gverts, _ = mesh_canon(*v.dump_mesh())
+    overts, _ = mesh_canon(*o64.dump_mesh())
+    common = sorted(set(gverts) & set(overts))
+    e_v = max(float(np.abs(gverts[k][:3] - overts[k][:3]).max()) for k in common) / p.voxel_size
+    cTw = np.linalg.inv(T.astype(np.float64)).astype(np.float32)
+    g_d, _, _ = v.raycast(cTw)
+    d64, _, _ = o64.raycast(cTw)
+    both = np.isfinite(g_d) & np.isfinite(d64)
+    e_d = float(np.abs(g_d[both] - d64[both]).max())
+    print(f"C1 vs FP64: max |dsdf| = {e_sdf:.3e} m ({e_sdf / p.truncation_distance:.2e} of truncation), "
+          f"max rel dw = {e_w:.3e}, vertex = {e_v:.3e} voxel over {len(common)}, depth = {e_d:.3e} m")
+    assert e_sdf < 1e-4 * p.truncation_distance and e_w < 1e-5
+    assert e_v < 1e-4 and e_d < 1e-4
+    assert both.sum() >= 0.999 * np.isfinite(g_d).sum()
+
+
+# ---------------------------------------------------------------------- C2
+def c2(n):
+    wl = scene.full_spline(n)
+    assert (wl.camera.width, wl.camera.height, wl.camera.fx) == (640, 480, 525.0)
+    # the benchmark's pools (bench.py workload_params)
+    p = config.params_for(wl, value_capacity=1 << 21, max_vertex_count=1 << 23, max_triangle_count=1 << 23,
+                          overflow_capacity=1 << 20, mesh_page_capacity=1 << 18)
+    assert (p.voxel_size, p.truncation_distance, p.bucket_count, p.enable_bayesian_update) == \
+        (np.float32(0.004), np.float32(0.012), 1 << 21, 1)
+    return wl, p
+
+
+TV_LAMBDA, TV_ITERS = 0.1, 20
+
+
+def test_c2_whole_chain_from_empty_exact(built):
+    wl, p = c2(5)
+    v = Volume(p)
+    o = Oracle(p, fp64=False)
+    gd = np.empty((p.rc_height, p.rc_width), np.float32)
+    for i in range(5):
+        d, T = wl.frame(i), wl.pose(i)
+        v.integrate_frame(d, T, tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA, ray_depth=gd)
+        od = o.frame(d, T, raycast=True, tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA)
+        assert same_set(v.candidates(), o.candidates()), f"C2 frame {i}: candidate sets differ"
+        nb = compare_volumes(v, o, ("sdf", "w", "a", "b"), f"C2 frame {i}")
+        nv, nt, gp, op = compare_mesh(v, o, f"C2 frame {i}")
+        pos_err = float(np.abs(gp[:, :3] - op[:, :3]).max()) / p.voxel_size if nv else 0.0
+        assert pos_err < 1e-4, pos_err
+        hit = np.isfinite(od)
+        assert np.array_equal(np.isfinite(gd), hit), f"C2 frame {i}: raycast hit masks differ"
+        assert bits_equal(gd[hit], od[hit]), f"C2 frame {i}: raycast depth differs"
+        print(f"C2 frame {i}: {nb} blocks, {len(v.candidates())} candidates, {nv} vertices, {nt} triangles, "
+              f"{int(hit.sum())} ray hits identical; vertex positions within {pos_err:.1e} voxel")
+    st = v.stats()
+    assert st["error"] == 0 and st["dropped_inserts"] == 0
+
+
+def test_c2_stagewise_on_fused_map(built):
+    wl, p = c2(21)
+    v = Volume(p)
+    for i in range(20):
+        v.integrate_frame(wl.frame(i), wl.pose(i), tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA)
+    o32, o64 = Oracle(p, fp64=False), Oracle(p, fp64=True)
+    d, T = wl.frame(20), wl.pose(20)
+    # input: TV on the GPU and in both oracles from the same preprocessed frame
+    v.set_frame(d, T)
+    v.denoise_tv(TV_LAMBDA, TV_ITERS)
+    gdep = v.depth()
+    o32.frame_set(d, T)
+    o32.denoise_tv(TV_LAMBDA, TV_ITERS)
+    assert bits_equal(gdep, o32.depth()), "TV: GPU and FP32 restatement differ"
+    o64.frame_set(d, T)
+    o64.denoise_tv(TV_LAMBDA, TV_ITERS)
+    d64 = o64.depth()
+    ok = np.isfinite(gdep)
+    assert np.array_equal(ok, np.isfinite(d64))
+    e_tv = float(np.abs(gdep[ok] - d64[ok]).max())
+    o64.set_depth(gdep)
+    # state of the 20-frame map
+    for o in (o32, o64):
+        hand_over(v, o, with_mesh=True)
+    nb0 = len(v.dump_blocks(fields=())[0])
+    # allocation and collection: exact sets
+    v.alloc_block_array()
+    o32.allocate()
+    gpos = v.dump_blocks(fields=())[0]
+    assert same_set(gpos, o32.blocks()[0]), "C2: block sets differ after allocation"
+    st = v.stats()
+    assert st["overflow_used"] > 0, "no overflow chain in use at 2^21 buckets"
+    v.collect_blocks_in_frustum()
+    o32.collect_frustum()
+    cand = v.candidates()
+    assert same_set(cand, o32.candidates()), "C2: candidate sets differ"
+    o64.allocate()
+    o64.set_candidates(cand)
+    # inlier prediction: identical bits
+    v.predict_outlier_ratio()
+    o32.predict_inlier()
+    gi = v.inlier()
+    assert bits_equal(gi, o32.inlier()), "C2: inlier ratios differ"
+    o64.set_inlier(gi)
+    # PSDF update: identical bits against FP32, bounds against FP64
+    v.update_blocks_bayesian()
+    o32.integrate_psdf()
+    o64.integrate_psdf()
+    compare_volumes(v, o32, ("sdf", "w", "a", "b"), "C2 PSDF update")
+    gpos, gf = v.dump_blocks()
+    p64, s64, w64, a64, b64 = o64.blocks()
+    gs, s6 = aligned(gpos, gf["sdf"], p64, s64)
+    gw, w6 = aligned(gpos, gf["w"], p64, w64)
+    m = w6 > 0
+    e_sdf = float(np.abs(gs - s6)[m].max())
+    e_w = float((np.abs(gw - w6)[m] / w6[m]).max())
+    e_ab = 0.0
+    for k, f64 in (("a", a64), ("b", b64)):
+        g, o = aligned(gpos, gf[k], p64, f64)
+        mm = np.abs(o) > 1e-3
+        e_ab = max(e_ab, float((np.abs(g - o)[mm] / np.abs(o[mm])).max()))
+    # meshing from the GPU's own state
+    hand_over(v, o32, with_mesh=True)
+    hand_over(v, o64, with_mesh=True)
+    for o in (o32, o64):
+        o.set_candidates(cand)
+    v.marching_cubes()
+    o32.mesh()
+    o64.mesh()
+    nv, nt, gp, op = compare_mesh(v, o32, "C2 marching cubes")
+    e_v32 = float(np.abs(gp[:, :3] - op[:, :3]).max()) / p.voxel_size
+    gverts, _ = mesh_canon(*v.dump_mesh())
+    overts, _ = mesh_canon(*o64.dump_mesh())
+    common = sorted(set(gverts) & set(overts))
+    e_v64 = max(float(np.abs(gverts[k][:3] - overts[k][:3]).max()) for k in common) / p.voxel_size
+    # raycast of the fused map
+    hand_over(v, o32)
+    hand_over(v, o64)
+    cTw = np.linalg.inv(T.astype(np.float64)).astype(np.float32)
+    rd, _, _ = v.raycast(cTw)
+    od, _, _ = o32.raycast(cTw)
+    hit = np.isfinite(od)
+    assert np.array_equal(np.isfinite(rd), hit), "C2: raycast hit masks differ"
+    assert bits_equal(rd[hit], od[hit]), "C2: raycast depth differs"
+    r64, _, _ = o64.raycast(cTw)
+    both = hit & np.isfinite(r64)
+    assert both.sum() >= 0.999 * hit.sum()
+    e_d = float(np.abs(rd[both] - r64[both]).max())
+    print(f"C2 frame 20 on the 20-frame map: {nb0} blocks before, {len(gpos)} after, {len(cand)} candidates, "
+          f"{st['overflow_used']} overflow entries, {nv} vertices, {nt} triangles, {int(hit.sum())} ray hits")
+    print(f"C2 vs FP64: TV depth {e_tv:.3e} m; sdf {e_sdf:.3e} m ({e_sdf / p.truncation_distance:.2e} of truncation, "
+          f"{e_sdf / 4.0:.2e} of the 4 m depth); weight {e_w:.3e} rel; a, b {e_ab:.3e} rel; "
+          f"vertex {e_v64:.3e} voxel (FP32 {e_v32:.1e}); raycast depth {e_d:.3e} m")
+    assert e_tv < 1e-5
+    assert e_sdf < 1e-5 * 4.0 and e_w < 1e-5
+    assert e_v32 < 1e-4 and e_v64 < 1e-4
+    assert e_d < 1e-4
+    assert v.stats()["error"] == 0
