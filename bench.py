@@ -130,7 +130,7 @@ class ClockSampler:
                 "reasons": reasons, "gpu": gpu, "samples": len(rows), "interval_ms": 50, "span": span}
 
 
-def workload_params(capacity_log2=21):
+def workload_params(capacity_log2=22):
     from meshhashing_gb300 import config, scene
     wl = scene.full_spline(8)
     pools = 1 << min(23, capacity_log2 + 2)
@@ -148,15 +148,15 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def bytes_per_launch(stage, nb, px, rpx, vwork, cube_blocks=0, mesh_blocks=0, predict_blocks=0):
+def bytes_per_launch(stage, nb, px, rpx, vwork, cube_blocks=0, mesh_blocks=0, predict_blocks=0, ray_blocks=None):
     """Algorithmic bytes one launch of a stage must move (per-frame averages of
     the blocks each kernel actually visits, counted on the device)."""
     if stage == "integrate":       # sdf, inv_sigma2, a, b read+write; depth + inlier images
         return nb * 512 * 32 + px * 8
     if stage == "predict":         # vertex slots of blocks with vertices; the inlier image
         return predict_blocks * 512 * 12 + px * 4
-    if stage == "raycast":         # 2 KB sdf + 16 B entry per block in view; depth, vertex, normal out
-        return nb * (512 * 4 + 16) + rpx * 36
+    if stage == "raycast":         # 2 KB sdf + 16 B entry per block the rays touch; depth, vertex, normal out
+        return (ray_blocks if ray_blocks is not None else nb) * (512 * 4 + 16) + rpx * 36
     if stage == "mesh":            # 9^3 corner tile of 4 fields + cube bytes for tiled blocks;
         # slots (12 + 20 B), cube and claim per voxel of paged blocks, twice; 32 B per vertex
         return cube_blocks * (729 * 16 + 512) + mesh_blocks * 512 * (12 + 20 + 1 + 4) * 2 + vwork * 32
@@ -217,17 +217,25 @@ def batch_params(spec, frames_run):
                              overflow_capacity=max(buckets // 4, 1024), mesh_page_capacity=max(cap // 64, 2048))
 
 
-def run_pose_refinement(vol, frames, poses, W, H, iterations=10):
-    """Frame-to-model refinement on the fused map: each frame starts from its
-    true pose perturbed by sigma 1 degree / 2 cm per axis (seeded) and runs
-    `iterations` Gauss-Newton steps (mh_refine_pose); plus one full-frame
+def run_pose_refinement(params, frames, poses, W, H, fused=100, refined=200, iterations=10):
+    """Differentiable-raycast pose refinement as the workload states it: a
+    fresh volume fuses frames 0..fused-1 (with the TV pre-filter), then each
+    of the next `refined` frames starts from its true pose perturbed by sigma
+    1 degree / 2 cm per axis (seeded) and runs `iterations` Gauss-Newton steps
+    (mh_refine_pose); the reference's point-to-PSDF tracker runs from the same
+    starts.  The map is not updated during refinement.  Also one full-frame
     raycast backward with voxel gradients."""
     import torch
+    from meshhashing_gb300 import Volume
     from meshhashing_gb300.pose import left_update, pose_error
+    vol = Volume(params)
+    for i in range(fused):
+        vol.integrate_frame(frames[i], poses[i], tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA)
+    torch.cuda.synchronize()
     rng = np.random.default_rng(77)
     start, final, ms = [], [], []
     p2p = {"reference": ([], []), "fixed_jacobian": ([], [])}
-    for d, T in zip(frames, poses):
+    for d, T in zip(frames[fused:fused + refined], poses[fused:fused + refined]):
         T_true = np.asarray(T, np.float64)
         xi = np.concatenate([rng.standard_normal(3) * 0.02, rng.standard_normal(3) * np.radians(1.0)])
         T0 = left_update(T_true, xi)
@@ -247,7 +255,7 @@ def run_pose_refinement(vol, frames, poses, W, H, iterations=10):
             T_p, _, _ = vol.track_point_to_psdf(T0, iterations=iterations, lam=lam, reference_jacobian=ref_j)
             p2p[key][0].append((time.perf_counter() - t0) * 1000.0)
             p2p[key][1].append(pose_error(T_p, T_true))
-    cTw = np.linalg.inv(np.asarray(poses[0], np.float64)).astype(np.float32)
+    cTw = np.linalg.inv(np.asarray(poses[fused], np.float64)).astype(np.float32)
     dl = torch.randn((H, W), generator=torch.Generator().manual_seed(3)).cuda()
     grad = torch.zeros(vol.params.value_capacity * 512, dtype=torch.float32, device="cuda")
     vol.raycast_backward(cTw, dl, None, grad)
@@ -255,18 +263,25 @@ def run_pose_refinement(vol, frames, poses, W, H, iterations=10):
     t0 = time.perf_counter()
     vol.raycast_backward(cTw, dl, None, grad)
     bw_ms = (time.perf_counter() - t0) * 1000.0
-    med = lambda xs, k: float(np.median([x[k] for x in xs]))
-    return {"frames": len(frames), "iterations": iterations, "ms_per_frame": float(np.median(ms)),
-            "start_error": {"mm": med(start, 0) * 1000.0, "deg": med(start, 1)},
-            "final_error": {"mm": med(final, 0) * 1000.0, "deg": med(final, 1)},
-            "final_error_max": {"mm": max(x[0] for x in final) * 1000.0, "deg": max(x[1] for x in final)},
+    vol.close()
+    del grad
+
+    def summary(errs):
+        mm = np.array([e[0] for e in errs]) * 1000.0
+        deg = np.array([e[1] for e in errs])
+        return {"median": {"mm": float(np.median(mm)), "deg": float(np.median(deg))},
+                "p95": {"mm": float(np.percentile(mm, 95)), "deg": float(np.percentile(deg, 95))},
+                "max": {"mm": float(mm.max()), "deg": float(deg.max())}}
+    return {"fused_frames": fused, "refined_frames": len(ms), "iterations": iterations,
+            "ms_per_frame": {"median": float(np.median(ms)), "p95": float(np.percentile(ms, 95))},
+            "start_error": summary(start), "final_error": summary(final),
             "raycast_backward_ms": bw_ms,
-            "point_to_psdf": {k: {"ms_per_frame": float(np.median(v[0])), "final_error": {"mm": med(v[1], 0) * 1000.0,
-                                                                                          "deg": med(v[1], 1)}}
+            "point_to_psdf": {k: {"ms_per_frame": float(np.median(v[0])), "final_error": summary(v[1])}
                               for k, v in p2p.items()},
-            "note": "median over frames; perturbation sigma 1 deg / 2 cm per axis; PSDF map of this run; "
-                    "point_to_psdf: the reference's tracker (MainEngine::Localizing) from the same starts, "
-                    "with its lambda 1e5 and J[2] = dD/dx, and with lambda 1 and the corrected Jacobian"}
+            "note": "frames 100..299 of the PSDF sequence on the map of frames 0..99; start poses perturbed by "
+                    "sigma 1 deg / 2 cm per axis; ms_per_frame is host wall time of the 10 iterations "
+                    "(synchronised); point_to_psdf: the reference's tracker (MainEngine::Localizing) from the same "
+                    "starts, with its lambda 1e5 and J[2] = dD/dx, and with lambda 1 and the corrected Jacobian"}
 
 
 def run_huber_tv(vol, peak, iterations=10):
@@ -466,6 +481,21 @@ def job_rate(world, steps, seconds):
     return world * steps / seconds
 
 
+def bench_config(prefuse, warmup, world=1):
+    """The workload of both arms (ours and --impl reference), identical so the
+    two lines describe the same frames."""
+    return {"workload": "psdf_640x480_4mm_room_spline", "resolution": [640, 480], "voxel_mm": 4,
+            "truncation_mm": 12, "buckets": 1 << 21, "tv_iterations": TV_ITERS, "prefuse_frames": prefuse,
+            "timed_frames": f"from frame {prefuse + warmup} on, one frame per step, after {warmup} warm-up frames",
+            "l2": "per-frame voxel working set (hundreds of thousands of 8 KB blocks) exceeds L2; no flush",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
+REF_MAX_FRAMES = 40
+POSE_FUSED, POSE_REFINED = 100, 200
+SEQ_FRAMES = 500   # the PSDF workload's sequence length
+
+
 def run_cpu_baseline(params, frames, poses, threads=None):
     """FP64 oracle on all host threads, from an empty volume."""
     from oracle import oracle as O
@@ -481,32 +511,40 @@ def run_cpu_baseline(params, frames, poses, threads=None):
 
 
 def run_reference(args, rank, world):
+    """The reference path's CPU implementation (the FP64 oracle restating the
+    reference's rules; the reference itself has no CPU path) on the same
+    frames as our arm: the map is pre-fused with the same prefuse + warm-up
+    frames (untimed), then the timed window's frames follow, one per step, up
+    to REF_MAX_FRAMES of them so the run stays within a few minutes."""
     if rank != 0:
         return
     import platform
     params = workload_params()
-    n = args.warmup + args.steps
-    frames, poses = gen_frames(list(range(n)), 500)
+    P, W = args.prefuse, args.warmup
+    n_time = max(1, min(args.steps, REF_MAX_FRAMES))
+    frames, poses = gen_frames(list(range(P + W + n_time)), SEQ_FRAMES)
     from oracle import oracle as O
     O.build()
     o = O.Oracle(params, fp64=True)
-    for i in range(args.warmup):
+    t_pre = time.perf_counter()
+    for i in range(P + W):
         o.frame(frames[i], poses[i], raycast=True, tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA)
+    t_pre = time.perf_counter() - t_pre
     t0 = time.perf_counter()
-    for i in range(args.warmup, n):
+    for i in range(P + W, P + W + n_time):
         o.frame(frames[i], poses[i], raycast=True, tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA)
     dt = time.perf_counter() - t0
-    fps = args.steps / dt
+    fps = n_time / dt
     cores = O.num_threads()
-    out = {"metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps, "higher_is_better": True,
+    sample = (f"frames {P + W}..{P + W + n_time - 1} (the first {n_time} of the timed window) on the map pre-fused "
+              f"from frames 0..{P + W - 1} ({t_pre:.0f} s, untimed); FP64 oracle, {cores} threads, "
+              f"{platform.machine()}")
+    out = {"metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": n_time,
+           "warmup": W, "ms_per_step": 1000.0 * dt / n_time, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "impl": "reference",
-           "config": {"workload": "psdf_640x480_4mm_room_spline", "frames": f"{args.warmup}..{n - 1} from empty",
-                      "tv_iterations": TV_ITERS, "parallelism": "cpu"},
-           "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
-                            "sample": f"frames {args.warmup}..{n - 1} of the sequence, FP64 oracle, "
-                                      f"{platform.machine()}"},
+           "config": bench_config(P, W, world),
+           "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port", "sample": sample},
            "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -514,7 +552,7 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--prefuse", type=int, default=40)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -526,7 +564,9 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=5)
     ap.add_argument("--stream-frames", type=int, default=STREAM_FRAMES,
                     help="frames of the floor-plan streaming measurement (0: skip it)")
-    ap.add_argument("--capacity-log2", type=int, default=21,
+    ap.add_argument("--pose-refined", type=int, default=POSE_REFINED,
+                    help="frames of the pose-refinement measurement after its 100 fused frames (0: skip it)")
+    ap.add_argument("--capacity-log2", type=int, default=22,
                     help="block pool size (2^n blocks); smaller values for profiler captures")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -539,10 +579,16 @@ def main():
         return
 
     K, W, P = args.steps, args.warmup, args.prefuse
-    R_POSE = 8
-    n_total = P + W + 3 * K + R_POSE
+    # Every frame comes from the workload's 500-frame sequence: the timed pass
+    # takes K frames, the per-stage pass and the e2e pass up to 100 each after
+    # it; the pose-refinement measurement uses frames 0..299.
+    K2 = K3 = min(K, 100)
+    if P + W + K + K2 + K3 > SEQ_FRAMES:
+        raise SystemExit(f"--prefuse + --warmup + --steps + 2 x min(steps, 100) must be <= {SEQ_FRAMES}")
+    n_total = SEQ_FRAMES
     # frames are rendered in a spawn pool before any CUDA call
-    frames, poses = gen_frames(list(range(n_total)), max(500, n_total))
+    n_pose = POSE_FUSED + args.pose_refined if args.pose_refined > 0 else 0
+    frames, poses = gen_frames(list(range(max(P + W + K + K2 + K3, n_pose))), SEQ_FRAMES)
     cpu_frames = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu_frames = (frames[:args.cpu_frames], poses[:args.cpu_frames])
@@ -563,7 +609,7 @@ def main():
     params = workload_params(args.capacity_log2)
     vol = Volume(params)
     Hh, Ww = params.height, params.width
-    dev_depth = torch.from_numpy(np.stack(frames[:P + W + 2 * K])).cuda()
+    dev_depth = torch.from_numpy(np.stack(frames[:P + W + K + K2])).cuda()
     rd = torch.empty((Hh, Ww), dtype=torch.float32, device="cuda")
     rv = torch.empty((Hh, Ww, 4), dtype=torch.float32, device="cuda")
     rn = torch.empty((Hh, Ww, 4), dtype=torch.float32, device="cuda")
@@ -601,28 +647,32 @@ def main():
     s0 = vol.stats()
     vol.profile(True)
     vol.profile_read()
-    for i in range(P + W + K, P + W + 2 * K):
+    for i in range(P + W + K, P + W + K + K2):
         step(i)
     prof = vol.profile_read()
     vol.profile(False)
     s1 = vol.stats()
+    # the raycast's block footprint (distinct blocks its rays look up) at the
+    # last profiled frame's pose, for the raycast byte model
+    ray_blocks = vol.raycast_footprint(np.linalg.inv(np.asarray(poses[P + W + K + K2 - 1], np.float64))
+                                       .astype(np.float32))
     clocks = sampler.stop((w0, w1), (w0, time.time()))
     ms = max_over_ranks(ms, world, "cuda")
     value = job_rate(world, K, ms / 1000.0)
 
     # e2e: host depth in (pinned), raycast depth back to host every frame
-    host_in = [torch.from_numpy(f).pin_memory() for f in frames[P + W + 2 * K:P + W + 3 * K]]
+    host_in = [torch.from_numpy(f).pin_memory() for f in frames[P + W + K + K2:P + W + K + K2 + K3]]
     host_out = torch.empty((Hh, Ww), dtype=torch.float32).pin_memory()
-    step_e2e = lambda j: vol.integrate_frame(host_in[j], poses[P + W + 2 * K + j], on_device=False,
+    step_e2e = lambda j: vol.integrate_frame(host_in[j], poses[P + W + K + K2 + j], on_device=False,
                                              tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA, ray_depth=host_out,
                                              outputs_on_device=False)
     barrier()
     t0 = time.perf_counter()
-    for j in range(K):
+    for j in range(K3):
         step_e2e(j)
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, "cuda")
-    e2e = job_rate(world, K, e2e_s)
+    e2e = job_rate(world, K3, e2e_s)
     s2 = vol.stats()
 
     passes = max(s1["mesh_passes"] - s0["mesh_passes"], 1)
@@ -630,7 +680,8 @@ def main():
     vwork = (s1["vertex_work_sum"] - s0["vertex_work_sum"]) / passes
     counts = {"cube_blocks": (s1["cube_blocks_sum"] - s0["cube_blocks_sum"]) / passes,
               "mesh_blocks": (s1["mesh_list_sum"] - s0["mesh_list_sum"]) / passes,
-              "predict_blocks": (s1["predict_blocks_sum"] - s0["predict_blocks_sum"]) / passes}
+              "predict_blocks": (s1["predict_blocks_sum"] - s0["predict_blocks_sum"]) / passes,
+              "ray_blocks": ray_blocks}
     px, rpx = Ww * Hh, params.rc_width * params.rc_height
     peak, peak_kind = peaks()
     stage_ms = {k: v[0] for k, v in prof.items()}
@@ -653,11 +704,12 @@ def main():
         if c:
             b = bytes_per_launch(k, nb, px, rpx, vwork, **counts)
             gbs = b / ((t_ms / c) / 1000.0) / 1e9 if t_ms > 0 else None
-            stages[k] = {"ms_per_frame": t_ms / K, "gbs": gbs, "frac": (gbs / peak) if gbs else None}
+            stages[k] = {"ms_per_frame": t_ms / K2, "gbs": gbs, "frac": (gbs / peak) if gbs else None}
 
-    pose = run_pose_refinement(vol, frames[P + W + 3 * K:], poses[P + W + 3 * K:], Ww, Hh)
     huber = run_huber_tv(vol, peak)
     vol.close()
+    pose = run_pose_refinement(params, frames, poses, Ww, Hh, POSE_FUSED, args.pose_refined) \
+        if args.pose_refined > 0 else None
     batched = None
     if bspecs:
         batched = run_batched(bspecs, bframes[0], bframes[1], BP, BW, BK)
@@ -676,11 +728,8 @@ def main():
         out = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": K, "warmup": W,
                "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                "dtype": "f32", "data": "synthetic",
-               "config": {"workload": "psdf_640x480_4mm_room_spline", "resolution": [Ww, Hh], "voxel_mm": 4,
-                          "truncation_mm": 12, "buckets": params.bucket_count, "prefuse_frames": P,
-                          "tv_iterations": TV_ITERS, "form": "plain (per-frame stream launches)",
-                          "l2": "per-frame working set (voxel state of ~%d blocks) exceeds L2" % int(nb),
-                          "parallelism": "replicas" if world > 1 else "single"},
+               "config": bench_config(P, W, world),
+               "form": "plain (per-frame stream launches)",
                "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": px * 4 + 64,
                        "d2h_bytes_per_step": rpx * 4},
                "gpu_launches": int(launches),

@@ -190,6 +190,13 @@ int mh_denoise_tv(mh_volume *v, float lambda, int iterations, void *stream);
 int mh_denoise_tv_static(const float *depth_in, float *depth_out, int width, int height, float lambda,
                          int iterations, void *stream);
 
+/* Introspection, no reference counterpart: raycasts from cTw (outputs
+ * discarded, the same march as mh_raycast) and counts the distinct blocks the
+ * rays looked up and found -- the raycast's block footprint, used by the
+ * byte model.  Allocates one byte per block of the pool on first use;
+ * synchronises `stream`. */
+int mh_raycast_footprint(mh_volume *v, const float cTw[16], int *blocks_touched, void *stream);
+
 /* One MainEngine frame (app/reconstruction.cc:82-100): frame set, optional TV
  * denoise (tv_iterations > 0), Mapping (main_engine.cc:100-154), Meshing
  * (:156-174), raycast into the caller's buffers (may be NULL) and the
@@ -252,6 +259,11 @@ int mh_dump_cubes(mh_volume *v, int n, const int32_t *pos, uint8_t *cube_idx);
 int mh_dump_block_meta(mh_volume *v, int n, const int32_t *pos, int32_t *life,
                        int32_t *inner, int32_t *boundary);
 int mh_dump_flags(mh_volume *v, int max_n, uint8_t *flags, int *n_out);
+/* Introspection, no reference counterpart: per block (INT32_MIN if absent)
+ * the count the library keeps of voxels whose sdf lies in (1e-30, 1e30);
+ * every sdf writer maintains it, and the raycast skips the trilinear
+ * gathers of samples whose corner blocks all count 512. */
+int mh_dump_positive_counts(mh_volume *v, int n, const int32_t *pos, int32_t *count);
 
 /* Per-stage GPU time, measured with CUDA events recorded on each stage's
  * stream around its launches (the reference's per-stage Timer and logging,

@@ -37,8 +37,8 @@ struct mh_batch {
   int n = 0;
   bool raycast = false;
   bool has_simple = false, has_psdf = false;
-  int alloc_tiles = 0, max_pixels = 0;
-  std::vector<int> alloc_tile0, pix0, rc_w, rc_h;
+  int alloc_tiles = 0, max_pixels = 0, tv_tiles = 0;
+  std::vector<int> alloc_tile0, tv_tile0, pix0, rc_w, rc_h;
   size_t pixels = 0;               // sum of the scenes' W x H
   // device: [Scene n][FrameConst n] and the host-depth staging
   char *d_block = nullptr;
@@ -115,7 +115,7 @@ static int enqueue(mh_batch *b, int p, bool host_depth, int tv_it, float lambda,
   mark(MH_STAGE_PREPROCESS);
   if ((r = launch_batch_preprocess(t, n, s)) != MH_OK) return r;
   mark(MH_STAGE_TV);
-  if (tv_it > 0 && (r = launch_batch_tv(t, n, b->max_pixels, lambda, tv_it, s)) != MH_OK) return r;
+  if (tv_it > 0 && (r = launch_batch_tv(t, n, b->tv_tiles, lambda, tv_it, s)) != MH_OK) return r;
   mark(MH_STAGE_ALLOC);
   if ((r = launch_batch_alloc(t, n, b->alloc_tiles, s)) != MH_OK) return r;
   mark(MH_STAGE_COLLECT);
@@ -168,6 +168,8 @@ int mh_batch_create(mh_volume *const *volumes, int count, int raycast, mh_batch 
     const int W = (int)v->hp.width, H = (int)v->hp.height;
     b->alloc_tile0.push_back(b->alloc_tiles);
     b->alloc_tiles += ((W + 15) / 16) * ((H + 15) / 16);
+    b->tv_tile0.push_back(b->tv_tiles);
+    b->tv_tiles += tv_tile_count(W, H);
     b->pix0.push_back((int)b->pixels);
     b->pixels += (size_t)W * H;
     b->max_pixels = std::max(b->max_pixels, W * H);
@@ -318,6 +320,7 @@ int mh_batch_step(mh_batch *b, const float *const *depth, int depth_on_device, c
     sc.ray_vert = reinterpret_cast<float4 *>(b->out_vert[i]);
     sc.ray_norm = reinterpret_cast<float4 *>(b->out_norm[i]);
     sc.alloc_tile0 = b->alloc_tile0[i];
+    sc.tv_tile0 = b->tv_tile0[i];
     sc.ray_tile0 = ray0[i];
     sc.pix0 = b->pix0[i];
     sc.active = act ? 1 : 0;

@@ -24,7 +24,8 @@ struct __align__(16) Scene {
   int alloc_tile0;           // first virtual tile of the scene in the alloc grid
   int ray_tile0;             // first virtual tile of the scene in the raycast grid
   int pix0;                  // first pixel of the scene in the concatenated pixel range
-  int pad[2];
+  int tv_tile0;              // first virtual tile of the scene in the tiled-TV grid
+  int pad;
 };
 
 __device__ __forceinline__ int flat_tid() { return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z); }

@@ -20,6 +20,7 @@ int launch_predict_inlier(const Dev &d, cudaStream_t s);
 int launch_mesh(const Dev &d, cudaStream_t s);
 
 int launch_raycast(const Dev &d, float *depth, float *vert4, float *norm4, cudaStream_t s);
+int launch_count_flags(const uint8_t *flags, int n, int *out, cudaStream_t s);
 
 int launch_gc_low_surfel(const Dev &d, cudaStream_t s);
 int launch_gc_starve(const Dev &d, cudaStream_t s);
@@ -30,7 +31,9 @@ int launch_denoise_tv(const Dev &d, float *tv, float lambda, int iterations, cud
 
 // batched twins: one launch per stage for every active scene of a scene table
 int launch_batch_preprocess(const Scene *t, int n, cudaStream_t s);
-int launch_batch_tv(const Scene *t, int n, int max_pixels, float lambda, int iterations, cudaStream_t s);
+int launch_batch_tv(const Scene *t, int n, int tv_tiles, float lambda, int iterations, cudaStream_t s);
+// tiles of the tiled TV kernel for a W x H frame
+int tv_tile_count(int W, int H);
 int launch_batch_alloc(const Scene *t, int n, int total_tiles, cudaStream_t s);
 int launch_batch_collect(const Scene *t, int n, cudaStream_t s);
 int launch_batch_predict(const Scene *t, int n, cudaStream_t s);

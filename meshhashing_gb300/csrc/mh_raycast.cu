@@ -6,26 +6,21 @@
 // and on a + to - sign change refines the hit with three regula-falsi steps
 // (BisectionIntersection, geometry/isosurface_intersection.h:21-55).  The
 // sample positions, the accumulation of t and every comparison follow the
-// reference's single-precision order exactly.
+// reference's single-precision order exactly, and so does every value the
+// output depends on.
 //
 // GB300 structure.  The march is bound by instruction issue and by the
 // latency of its dependent loads, not by HBM bandwidth, so the work per
 // sample is what is cut, never the sample sequence itself:
-//  * one gather for every sample: the eight corners' blocks come from a
-//    per-ray table of the first corner block's 2x2x2 neighbourhood, filled by
-//    hash lookups only when a sample first needs an entry.  Samples whose
-//    corners straddle a block face take the same instructions as the others,
-//    so the lanes of a warp stay together (a separate slow path for the third
-//    of samples that straddle a face cost 1.45x in time).
-//  * one out-of-line sampler serves the march, the refinement and the
-//    gradient.  Inlined three times the kernel outgrew the instruction cache
-//    and its register budget (measured 1.5x slower).
-//  * empty-space skip: when the block holding a sample's first corner is
-//    missing, every later sample of the ray whose first corner falls in that
-//    block fails the same way.  The t interval in which the ray stays inside
-//    the block shrunk by a margin (0.1 voxel plus the float error of the
-//    position) is computed once, and samples inside it only advance t
-//    (t += step, the same accumulation as the full loop).
+//  * all state in registers: one sampler, inlined once, serves the march, the
+//    lazily evaluated previous sample, the regula falsi and the gradient
+//    (a phase variable picks the next position); the first corner's 2x2x2
+//    block neighbourhood is a register table filled by hash lookups only
+//    when a sample first needs an entry, so a sample's eight corners come
+//    from one branch-uniform gather;
+//  * exact skips (see ray_march): samples whose corner blocks hold only
+//    positive voxels are never gathered, and the t intervals inside missing
+//    blocks and inside all-positive blocks only advance t;
 //  * 16x8-pixel CTAs keep neighbouring rays in one warp; they walk the same
 //    blocks at about the same t.
 #include "mh_internal.cuh"
@@ -49,17 +44,50 @@ struct RayCache {
   }
 };
 
-enum { RS_OK = 0, RS_MISS0 = 1, RS_MISS0_NEW = 2, RS_MISS = 3 };
+}  // namespace
 
-// GetSpatialValue (geometry/spatial_query.h:23-66) for the raycast: the same
-// corners, weights and summation order as spatial_sample.  Every sample runs
-// the same gather: corner i lies in block b0 + (mx & ex, my & ey, mz & ez),
-// where e is the block step between the two corner voxels of each axis, and
-// the up to eight blocks of b0's 2x2x2 neighbourhood are looked up once per
-// b0 and only when a sample needs them.  Returns RS_OK, or why the sample
-// failed: its first corner's block is missing (RS_MISS0_NEW when that block
-// was just looked up) or another corner's block is missing.
-__device__ __noinline__ int ray_sample(const Dev &d, RayCache &c, F3 pos, float &sdf) {
+// ------------------------------------------------------------------ forward
+// The forward march keeps its whole state in registers: one sampler is
+// inlined once, and a phase variable chooses where the next sample goes --
+// the march itself, the lazily evaluated previous sample, the three
+// regula-falsi steps, the six gradient samples of the normal.  The first
+// corner's 2x2x2 block neighbourhood is a register table with three masks
+// (looked up, missing, all voxels positive), filled by hash lookups only when
+// a sample first needs an entry.
+//
+// Skips, all exact.  A march sample is only needed for its sign, unless it is
+// negative right after a positive one; a sample whose corner blocks hold
+// only positive voxels (per-block count posc == 512) is positive and valid,
+// so its gather is skipped and it becomes the "previous sample" lazily: its
+// value is computed only when the next evaluated sample is negative.  Two
+// kinds of t interval are skipped with nothing but t += step: where the
+// first corner's block is missing (every sample invalid), and the interior
+// of an all-positive block where all eight corners lie in that block (every
+// sample valid and positive).
+namespace {
+
+enum { SM_OK = 0, SM_POS = 1, SM_MISS0 = 2, SM_MISS0_NEW = 3, SM_MISS = 4 };
+
+struct Nbhd {
+  int bx, by, bz;    // block of the first corner of the last sample
+  unsigned looked;   // bit n: block n = (bx, by, bz) + (n & 1, n >> 1 & 1, n >> 2 & 1) looked up
+  unsigned miss;     // bit n: block n is missing
+  unsigned pos;      // bit n: every voxel of block n is positive
+  int p[8];          // block indices, indexed with constants only (registers)
+  __device__ __forceinline__ void init() {
+    bx = by = bz = 0x7fffffff;
+    looked = miss = pos = 0u;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) p[j] = -1;
+  }
+};
+
+// GetSpatialValue (geometry/spatial_query.h:23-66) with the same corners,
+// weights and summation order as spatial_sample.  Returns SM_OK with the
+// value in s, SM_POS when allow_pos and every corner block is all-positive
+// (value not computed), or why the sample is invalid.  b0_fresh: the first
+// corner's block was looked up by this call.
+__device__ __forceinline__ int nb_sample(const Dev &d, Nbhd &c, F3 pos, bool allow_pos, float &s, bool &b0_fresh) {
   const float off = d.p.voxel_size;
   const float vs = d.p.voxel_size;
   const float qx = pos.x / vs, qy = pos.y / vs, qz = pos.z / vs;
@@ -69,52 +97,81 @@ __device__ __noinline__ int ray_sample(const Dev &d, RayCache &c, F3 pos, float 
   corner_pair(pos.x, off, vs, fx, rx, v0x, v1x);
   corner_pair(pos.y, off, vs, fy, ry, v0y, v1y);
   corner_pair(pos.z, off, vs, fz, rz, v0z, v1z);
-  const int b0x = vox2blk(v0x), b0y = vox2blk(v0y), b0z = vox2blk(v0z);
+  // VoxelToBlock: floor division by 8 (geometry_helper.h:82-90)
+  const int b0x = v0x >> 3, b0y = v0y >> 3, b0z = v0z >> 3;
   if (b0x != c.bx || b0y != c.by || b0z != c.bz) {
     c.bx = b0x, c.by = b0y, c.bz = b0z;
-    c.valid = 0;
+    c.looked = c.miss = c.pos = 0u;
   }
-  const int ex = vox2blk(v1x) - b0x, ey = vox2blk(v1y) - b0y, ez = vox2blk(v1z) - b0z;
-  // blocks the eight corners use: every subset of the axes that step
-  int need = 1;
+  const int ex = (v1x >> 3) - b0x, ey = (v1y >> 3) - b0y, ez = (v1z >> 3) - b0z;
+  unsigned need = 1u;
   if (ex) need |= need << 1;
   if (ey) need |= need << 2;
   if (ez) need |= need << 4;
-  const int fresh = need & ~c.valid;
-  if (fresh & 1) c.p[0] = hash_find(d, b0x, b0y, b0z);
-  c.valid |= fresh & 1;
-  if (c.p[0] < 0) return (fresh & 1) ? RS_MISS0_NEW : RS_MISS0;
-  for (int todo = fresh & ~1; todo; todo &= todo - 1) {
-    const int n = __ffs(todo) - 1;
-    c.p[n] = hash_find(d, b0x + (n & 1), b0y + ((n >> 1) & 1), b0z + ((n >> 2) & 1));
+  unsigned fresh = need & ~c.looked;
+  b0_fresh = fresh & 1u;
+  if (b0_fresh) {
+    const int q = hash_find(d, b0x, b0y, b0z);
+    c.p[0] = q;
+    if (q >= 0 && d.touch) d.touch[q] = 1;
+    if (q < 0) c.miss |= 1u;
+    else if (__ldg(d.posc + q) == MH_BLOCK_VOXELS) c.pos |= 1u;
+    c.looked |= 1u;
+    fresh &= ~1u;
   }
-  c.valid |= fresh;
-  for (int m = need & ~1; m; m &= m - 1)
-    if (c.p[__ffs(m) - 1] < 0) return RS_MISS;
-  const float w0x = 1.0f - rx, w0y = 1.0f - ry, w0z = 1.0f - rz;
+  if (c.miss & 1u) return b0_fresh ? SM_MISS0_NEW : SM_MISS0;
+  while (fresh) {
+    const int n = __ffs(fresh) - 1;
+    fresh &= fresh - 1;
+    const int q = hash_find(d, b0x + (n & 1), b0y + ((n >> 1) & 1), b0z + ((n >> 2) & 1));
+#pragma unroll
+    for (int j = 1; j < 8; ++j)
+      if (j == n) c.p[j] = q;
+    if (q >= 0 && d.touch) d.touch[q] = 1;
+    if (q < 0) c.miss |= 1u << n;
+    else if (__ldg(d.posc + q) == MH_BLOCK_VOXELS) c.pos |= 1u << n;
+  }
+  c.looked |= need;
+  if (need & c.miss) return SM_MISS;
+  if (allow_pos && (need & ~c.pos) == 0u) return SM_POS;
+  // block of each corner (mx, my, mz): p[(mx & ex) | (my & ey) << 1 | (mz & ez) << 2]
+  const int B0 = c.p[0];
+  const int BX = ex ? c.p[1] : B0;
+  const int BY = ey ? c.p[2] : B0;
+  const int BXY = ey ? (ex ? c.p[3] : c.p[2]) : BX;
+  const int BZ = ez ? c.p[4] : B0;
+  const int BXZ = ez ? (ex ? c.p[5] : c.p[4]) : BX;
+  const int BYZ = ez ? (ey ? c.p[6] : c.p[4]) : BY;
+  const int BXYZ = ez ? (ey ? (ex ? c.p[7] : c.p[6]) : (ex ? c.p[5] : c.p[4])) : BXY;
+  const int blk[8] = {B0, BZ, BY, BYZ, BX, BXZ, BXY, BXYZ};
   // local voxel coordinates of the two corners of each axis
-  const int l0x = v0x - b0x * MH_BLOCK_SIDE, l1x = v1x - (b0x + ex) * MH_BLOCK_SIDE;
-  const int l0y = v0y - b0y * MH_BLOCK_SIDE, l1y = v1y - (b0y + ey) * MH_BLOCK_SIDE;
-  const int l0z = v0z - b0z * MH_BLOCK_SIDE, l1z = v1z - (b0z + ez) * MH_BLOCK_SIDE;
-  float s = 0.0f;
+  const int l0x = v0x & 7, l1x = v1x & 7;
+  const int yz[4] = {(v0y & 7) * 8 + (v0z & 7) * 64, (v0y & 7) * 8 + (v1z & 7) * 64,
+                     (v1y & 7) * 8 + (v0z & 7) * 64, (v1y & 7) * 8 + (v1z & 7) * 64};
+  const float w0x = 1.0f - rx, w0y = 1.0f - ry, w0z = 1.0f - rz;
+  const float wxy[4] = {w0x * w0y, w0x * ry, rx * w0y, rx * ry};
+  float v[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    const int mx = (i & 4) > 0, my = (i & 2) > 0, mz = (i & 1) > 0;
-    const float w = (mx ? rx : w0x) * (my ? ry : w0y) * (mz ? rz : w0z);
-    const int n = (mx & ex) | ((my & ey) << 1) | ((mz & ez) << 2);
-    const int li = (mx ? l1x : l0x) + (my ? l1y : l0y) * MH_BLOCK_SIDE +
-                   (mz ? l1z : l0z) * MH_BLOCK_SIDE * MH_BLOCK_SIDE;
-    s += w * __ldg(d.sdf + (size_t)c.p[n] * MH_BLOCK_VOXELS + li);
+    const int mx = (i >> 2) & 1, lyz = i & 3;
+    v[i] = __ldg(d.sdf + (size_t)(blk[i] * MH_BLOCK_VOXELS + (mx ? l1x : l0x) + yz[lyz]));
   }
-  sdf = s;
-  return RS_OK;
+  float acc = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int mz = i & 1;
+    acc += wxy[i >> 1] * (mz ? rz : w0z) * v[i];
+  }
+  s = acc;
+  return SM_OK;
 }
 
-// One axis of the slab test: narrows [lo, hi] to the t for which the ray's
-// coordinate lies strictly inside (a, b).
-__device__ __forceinline__ void slab(float o, float dir, float a, float b, float &lo, float &hi) {
+// One axis of a slab test with the direction's reciprocal: narrows [lo, hi]
+// to the t for which the ray's coordinate lies inside (a, b).  The bounds
+// carry a few ulp of rounding; the box margins below absorb them.
+__device__ __forceinline__ void slab_r(float o, float dir, float idir, float a, float b, float &lo, float &hi) {
   if (dir != 0.0f) {
-    const float t1 = (a - o) / dir, t2 = (b - o) / dir;
+    const float t1 = (a - o) * idir, t2 = (b - o) * idir;
     lo = fmaxf(lo, fminf(t1, t2));
     hi = fminf(hi, fmaxf(t1, t2));
   } else if (!(o > a && o < b)) {
@@ -124,15 +181,16 @@ __device__ __forceinline__ void slab(float o, float dir, float a, float b, float
 }
 
 // t interval in which every sample of the ray cam + t * wd has its first
-// corner in block (bx, by, bz).  A position at least 0.1 voxel inside the
-// block's faces has floor(p / v) -- and, where p / v is within 0.01 of an
-// integer, round-half-away(p / v - 1/2) -- inside the block.  The margin adds
-// 8 units in the last place of the coordinates for the rounding of the
-// position and of the interval ends.
-__device__ __forceinline__ void miss_interval(const DevParams &p, int bx, int by, int bz, F3 cam, F3 wd, float &lo,
-                                              float &hi) {
+// corner voxel at local coordinates [0, cells) of block (bx, by, bz) on each
+// axis: cells = 8 puts the first corner in the block, cells = 7 all eight
+// corners.  A coordinate at least 0.1 voxel inside those faces has floor(p / v)
+// -- and, where p / v is within 0.01 of an integer, round-half-away(p / v -
+// 1/2) -- in range; the margin adds 8 units in the last place of the
+// coordinates for the rounding of the position and of the interval ends.
+__device__ __forceinline__ void block_interval(const DevParams &p, int bx, int by, int bz, int cells, F3 cam, F3 wd,
+                                               F3 iwd, float &lo, float &hi) {
   const float vs = p.voxel_size;
-  const float side = (float)MH_BLOCK_SIDE * vs;
+  const float side = (float)MH_BLOCK_SIDE * vs, span = (float)cells * vs;
   lo = -__int_as_float(0x7f800000);
   hi = __int_as_float(0x7f800000);
   const float ax = (float)(bx * MH_BLOCK_SIDE) * vs, ay = (float)(by * MH_BLOCK_SIDE) * vs,
@@ -140,34 +198,160 @@ __device__ __forceinline__ void miss_interval(const DevParams &p, int bx, int by
   const float mx = 0.1f * vs + 5e-7f * (fabsf(ax) + side + fabsf(cam.x));
   const float my = 0.1f * vs + 5e-7f * (fabsf(ay) + side + fabsf(cam.y));
   const float mz = 0.1f * vs + 5e-7f * (fabsf(az) + side + fabsf(cam.z));
-  slab(cam.x, wd.x, ax + mx, ax + side - mx, lo, hi);
-  slab(cam.y, wd.y, ay + my, ay + side - my, lo, hi);
-  slab(cam.z, wd.z, az + mz, az + side - mz, lo, hi);
-}
-
-// GetSpatialSDFGradient: central differences h = half a voxel either side
-// (spacing = 0.5); a wider spacing gives a smoother normal
-__device__ __forceinline__ bool ray_gradient(const Dev &d, RayCache &c, F3 pos, F3 &g, float spacing = 0.5f) {
-  const float h = spacing * d.p.voxel_size;
-  const float vs = d.p.voxel_size;
-  float gx = 0.0f, gy = 0.0f, gz = 0.0f;
-#pragma unroll 1
-  for (int i = 0; i < 3; ++i) {
-    F3 dm = f3(pos.x - (i == 0 ? h : 0.0f), pos.y - (i == 1 ? h : 0.0f), pos.z - (i == 2 ? h : 0.0f));
-    F3 dp = f3(pos.x + (i == 0 ? h : 0.0f), pos.y + (i == 1 ? h : 0.0f), pos.z + (i == 2 ? h : 0.0f));
-    float sn, sp;
-    if (ray_sample(d, c, dm, sn) != RS_OK) return false;
-    if (ray_sample(d, c, dp, sp) != RS_OK) return false;
-    const float gi = (sp - sn) / (vs * (2.0f * spacing));
-    gx = i == 0 ? gi : gx;
-    gy = i == 1 ? gi : gy;
-    gz = i == 2 ? gi : gz;
-  }
-  g = f3(gx, gy, gz);
-  return true;
+  slab_r(cam.x, wd.x, iwd.x, ax + mx, ax + span - mx, lo, hi);
+  slab_r(cam.y, wd.y, iwd.y, ay + my, ay + span - my, lo, hi);
+  slab_r(cam.z, wd.z, iwd.z, az + mz, az + span - mz, lo, hi);
 }
 
 }  // namespace
+
+// What one ray's march found: whether a hit was accepted, the two march
+// samples around the zero crossing, which end each regula-falsi step
+// replaced, the last regula-falsi point and, when asked, the spatial
+// gradient at that point (g_ok false if a gradient sample was invalid).
+struct March {
+  bool hit, g_ok;
+  float t0, t1, m;
+  int side;  // bit k: regula-falsi step k replaced the left end
+  F3 g;
+};
+
+// RayCaster::CastKernel's march (visualization/ray_caster.cu:62-150) for the
+// ray cam + t * wd, t from t_min while t < t_max, with the exact skips
+// described above; spacing > 0 also evaluates GetSpatialSDFGradient at the hit
+// with central differences `spacing` voxels either side (spatial_query.h:68-97
+// uses 0.5).
+__device__ __forceinline__ March ray_march(const Dev &d, F3 cam, F3 wd, float t_min, float t_max, float spacing) {
+  const DevParams &p = d.p;
+  const F3 iwd = f3(wd.x != 0.0f ? 1.0f / wd.x : 0.0f, wd.y != 0.0f ? 1.0f / wd.y : 0.0f,
+                    wd.z != 0.0f ? 1.0f / wd.z : 0.0f);
+  const float vs = p.voxel_size;
+  const float step = p.raycast_step;
+  enum { PH_MARCH, PH_PREV, PH_REFINE, PH_GRAD };
+  March out;
+  out.hit = false, out.g_ok = false, out.t0 = out.t1 = out.m = 0.0f, out.side = 0;
+  out.g = f3(0.0f, 0.0f, 0.0f);
+  Nbhd c;
+  c.init();
+  int phase = PH_MARCH, k = 0, side = 0;
+  bool have_prev = false, prev_lazy = false, skip_pos = false;
+  float prev_sdf = 0.0f, prev_t = 0.0f, skip_lo = 1.0f, skip_hi = 0.0f;
+  float t = t_min, cur_s = 0.0f, l = 0.0f, r = 0.0f, ls = 0.0f, rs = 0.0f, m = 0.0f, g_minus = 0.0f;
+  F3 iso = f3(0.0f, 0.0f, 0.0f);
+#pragma unroll 1
+  while (true) {
+    F3 pos;
+    if (phase == PH_MARCH) {
+      if (t > skip_lo && t < skip_hi && t < t_max) {
+        float last;
+#pragma unroll 1
+        do {
+          last = t;
+          t += step;
+        } while (t < skip_hi && t < t_max);
+        if (skip_pos) have_prev = true, prev_lazy = true, prev_t = last;
+      }
+      if (!(t < t_max)) break;
+      pos = f3(cam.x + t * wd.x, cam.y + t * wd.y, cam.z + t * wd.z);
+    } else if (phase == PH_PREV) {
+      pos = f3(cam.x + prev_t * wd.x, cam.y + prev_t * wd.y, cam.z + prev_t * wd.z);
+    } else if (phase == PH_REFINE) {
+      m = l + (ls / (ls - rs)) * (r - l);
+      pos = f3(cam.x + m * wd.x, cam.y + m * wd.y, cam.z + m * wd.z);
+    } else {
+      // axis k / 2, minus side first
+      const float h = spacing * vs;
+      const int ax = k >> 1;
+      if (k & 1) pos = f3(iso.x + (ax == 0 ? h : 0.0f), iso.y + (ax == 1 ? h : 0.0f), iso.z + (ax == 2 ? h : 0.0f));
+      else pos = f3(iso.x - (ax == 0 ? h : 0.0f), iso.y - (ax == 1 ? h : 0.0f), iso.z - (ax == 2 ? h : 0.0f));
+    }
+    float s = 0.0f;
+    bool b0_fresh = false;
+    const int res = nb_sample(d, c, pos, phase == PH_MARCH, s, b0_fresh);
+    if (phase == PH_MARCH) {
+      if (b0_fresh) {
+        if (res == SM_MISS0_NEW) {
+          block_interval(p, c.bx, c.by, c.bz, MH_BLOCK_SIDE, cam, wd, iwd, skip_lo, skip_hi);
+          skip_pos = false;
+        } else if (c.pos & 1u) {
+          block_interval(p, c.bx, c.by, c.bz, MH_BLOCK_SIDE - 1, cam, wd, iwd, skip_lo, skip_hi);
+          skip_pos = true;
+        }
+      }
+      if (res == SM_POS) {
+        have_prev = true, prev_lazy = true, prev_t = t;
+      } else if (res == SM_OK) {
+        if (have_prev && s < 0.0f && (prev_lazy || prev_sdf > 0.0f)) {
+          // zero crossing: the previous sample's value is needed first
+          cur_s = s;
+          if (prev_lazy) {
+            phase = PH_PREV;
+          } else {
+            l = prev_t, r = t, ls = prev_sdf, rs = s, k = 0, side = 0;
+            phase = PH_REFINE;
+          }
+          continue;
+        }
+        prev_sdf = s, prev_t = t, have_prev = true, prev_lazy = false;
+      }
+      t += step;
+      continue;
+    }
+    if (phase == PH_PREV) {
+      prev_lazy = false;
+      if (res != SM_OK || !(s > 0.0f)) {
+        // cannot happen while every sdf writer keeps posc exact
+        set_error(d, MH_ERR_STATE);
+        prev_sdf = cur_s, prev_t = t, have_prev = true;
+        t += step;
+        phase = PH_MARCH;
+        continue;
+      }
+      prev_sdf = s;
+      l = prev_t, r = t, ls = prev_sdf, rs = cur_s, k = 0, side = 0;
+      phase = PH_REFINE;
+      continue;
+    }
+    if (phase == PH_REFINE) {
+      bool hit = false;
+      if (res == SM_OK) {
+        if (ls * s > 0.0f) l = m, ls = s, side |= 1 << k;
+        else r = m, rs = s;
+        if (++k < 3) continue;
+        hit = fabsf(prev_sdf - cur_s) < p.sample_sdf_threshold && fabsf(cur_s) < p.sdf_threshold;
+      }
+      if (!hit) {
+        // BisectionIntersection failed or the sample is not good enough:
+        // the march goes on from this sample (ray_caster.cu:119-122)
+        prev_sdf = cur_s, prev_t = t, have_prev = true, prev_lazy = false;
+        t += step;
+        phase = PH_MARCH;
+        continue;
+      }
+      out.hit = true, out.t0 = prev_t, out.t1 = t, out.m = m, out.side = side;
+      if (!(spacing > 0.0f)) break;
+      iso = f3(cam.x + m * wd.x, cam.y + m * wd.y, cam.z + m * wd.z);
+      k = 0;
+      out.g_ok = true;
+      phase = PH_GRAD;
+      continue;
+    }
+    // PH_GRAD
+    if (res != SM_OK) {
+      out.g_ok = false;
+      break;
+    }
+    if (!(k & 1)) {
+      g_minus = s;
+    } else {
+      const float gi = (s - g_minus) / (vs * (2.0f * spacing));
+      const int ax = k >> 1;
+      out.g = f3(ax == 0 ? gi : out.g.x, ax == 1 ? gi : out.g.y, ax == 2 ? gi : out.g.z);
+    }
+    if (++k == 6) break;
+  }
+  return out;
+}
 
 template <int TX, int TY>
 __device__ __forceinline__ void raycast_body(const Dev &d, int tile_x, int tile_y, float *out_depth, float4 *out_vert, float4 *out_norm) {
@@ -192,64 +376,21 @@ __device__ __forceinline__ void raycast_body(const Dev &d, int tile_x, int tile_
   const float t_max = p.max_raycast_depth / cd.z;
   const F3 cam = mul_pt(wTc, f3(0.0f, 0.0f, 0.0f));
   const F3 wd = normalize3(mul_dir(wTc, cd));
-
-  RayCache c;
-  c.init();
-  bool have_prev = false;
-  float prev_sdf = 0.0f, prev_t = 0.0f;
-  float skip_lo = 1.0f, skip_hi = 0.0f;
-  const float step = p.raycast_step;
-  float t = t_min;
-#pragma unroll 1
-  while (true) {
-#pragma unroll 1
-    while (t > skip_lo && t < skip_hi && t < t_max) t += step;
-    if (!(t < t_max)) break;
-    float s;
-    const int rs = ray_sample(d, c, f3(cam.x + t * wd.x, cam.y + t * wd.y, cam.z + t * wd.z), s);
-    if (rs != RS_OK) {
-      if (rs == RS_MISS0_NEW) miss_interval(p, c.bx, c.by, c.bz, cam, wd, skip_lo, skip_hi);
-      t += step;
-      continue;
+  const bool want_normal = p.enable_gradients && out_norm;
+  const March mr = ray_march(d, cam, wd, t_min, t_max, want_normal ? 0.5f : 0.0f);
+  if (mr.hit) {
+    const float dz = mr.m * cd.z;
+    o_depth = dz;
+    o_vert = make_float4(dz * rx, dz * ry, dz, 1.0f);
+    if (want_normal) {
+      const F3 g = mr.g;
+      const float len = sqrtf(dot3(g, g));
+      F3 nn = f3(0.0f, 0.0f, 0.0f);
+      if (mr.g_ok && len > 0.0f) nn = f3(g.x / len, g.y / len, g.z / len);
+      nn = f3(-nn.x, -nn.y, -nn.z);
+      const F3 nc = mul_dir(cTw, nn);
+      o_norm = make_float4(nc.x, nc.y, nc.z, 1.0f);
     }
-    if (have_prev && prev_sdf > 0.0f && s < 0.0f) {
-      float l = prev_t, r = t, m = (l + r) * 0.5f;
-      float ls = prev_sdf, rs_ = s;
-      bool found = true;
-#pragma unroll 1
-      for (int k = 0; k < 3; ++k) {
-        m = l + (ls / (ls - rs_)) * (r - l);
-        float ms;
-        if (ray_sample(d, c, f3(cam.x + m * wd.x, cam.y + m * wd.y, cam.z + m * wd.z), ms) != RS_OK) {
-          found = false;
-          break;
-        }
-        if (ls * ms > 0.0f) {
-          l = m, ls = ms;
-        } else {
-          r = m, rs_ = ms;
-        }
-      }
-      if (found && fabsf(prev_sdf - s) < p.sample_sdf_threshold && fabsf(s) < p.sdf_threshold) {
-        const float dz = m * cd.z;
-        o_depth = dz;
-        o_vert = make_float4(dz * rx, dz * ry, dz, 1.0f);
-        if (p.enable_gradients && out_norm) {
-          const F3 iso = f3(cam.x + m * wd.x, cam.y + m * wd.y, cam.z + m * wd.z);
-          F3 g;
-          const bool ok = ray_gradient(d, c, iso, g);
-          const float len = sqrtf(dot3(g, g));
-          F3 nn = f3(0.0f, 0.0f, 0.0f);
-          if (ok && len > 0.0f) nn = f3(g.x / len, g.y / len, g.z / len);
-          nn = f3(-nn.x, -nn.y, -nn.z);
-          const F3 nc = mul_dir(cTw, nn);
-          o_norm = make_float4(nc.x, nc.y, nc.z, 1.0f);
-        }
-        break;
-      }
-    }
-    prev_sdf = s, prev_t = t, have_prev = true;
-    t += step;
   }
   if (out_depth) out_depth[pix] = o_depth;
   if (out_vert) out_vert[pix] = o_vert;
@@ -259,7 +400,7 @@ __global__ void __launch_bounds__(RC_TX *RC_TY) k_raycast(Dev d, float *out_dept
 // batched raycast over the scenes' concatenated TX x TY tiles; the tile shape
 // is an autotuned choice (the scene table's ray_tile0 follows it)
 template <int TX, int TY>
-__global__ void __launch_bounds__(TX *TY, 65536 / (TX * TY * 72)) k_raycast_b(const Scene *t, int n, int total) {
+__global__ void __launch_bounds__(TX *TY, 4) k_raycast_b(const Scene *t, int n, int total) {
   each_tile(t, n, total, &Scene::ray_tile0, [&](const Scene &c, int lt) {
     const int tw = (c.d.p.rc_width + TX - 1) / TX;
     raycast_body<TX, TY>(c.d, lt % tw, lt / tw, c.ray_depth, c.ray_vert, c.ray_norm);
@@ -281,6 +422,19 @@ int launch_raycast_batch(const Scene *t, int n, int total, int shape, cudaStream
     case 2: k_raycast_b<32, 4><<<grid, dim3(32, 4), 0, s>>>(t, n, total); break;
     default: k_raycast_b<16, 8><<<grid, dim3(16, 8), 0, s>>>(t, n, total); break;
   }
+  mh_count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+
+// number of nonzero bytes of flags[0, n) added to *out
+__global__ void k_count_flags(const uint8_t *flags, int n, int *out) {
+  int c = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) c += flags[i] != 0;
+  c = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+int launch_count_flags(const uint8_t *flags, int n, int *out, cudaStream_t s) {
+  k_count_flags<<<std::max(1, std::min((n + 255) / 256, mh_sm_count() * 8)), 256, 0, s>>>(flags, n, out);
   mh_count_launches(1);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }
@@ -381,53 +535,6 @@ struct RayTrace {
   float t0, t1;  // the bracketing samples
   int side;      // bit k: regula-falsi step k replaced the left end
 };
-
-// the forward's march (k_raycast), recording its decisions instead of outputs
-__device__ __noinline__ RayTrace ray_trace(const Dev &d, RayCache &c, F3 cam, F3 wd, float t_min, float t_max) {
-  const DevParams &p = d.p;
-  RayTrace tr{false, 0.0f, 0.0f, 0};
-  bool have_prev = false;
-  float prev_sdf = 0.0f, prev_t = 0.0f;
-  float skip_lo = 1.0f, skip_hi = 0.0f;
-  const float step = p.raycast_step;
-  float t = t_min;
-  while (true) {
-    while (t > skip_lo && t < skip_hi && t < t_max) t += step;
-    if (!(t < t_max)) break;
-    float s;
-    const int rs = ray_sample(d, c, f3(cam.x + t * wd.x, cam.y + t * wd.y, cam.z + t * wd.z), s);
-    if (rs != RS_OK) {
-      if (rs == RS_MISS0_NEW) miss_interval(p, c.bx, c.by, c.bz, cam, wd, skip_lo, skip_hi);
-      t += step;
-      continue;
-    }
-    if (have_prev && prev_sdf > 0.0f && s < 0.0f) {
-      float l = prev_t, r = t, ls = prev_sdf, rs_ = s;
-      bool found = true;
-      int side = 0;
-      for (int k = 0; k < 3; ++k) {
-        const float m = l + (ls / (ls - rs_)) * (r - l);
-        float ms;
-        if (ray_sample(d, c, f3(cam.x + m * wd.x, cam.y + m * wd.y, cam.z + m * wd.z), ms) != RS_OK) {
-          found = false;
-          break;
-        }
-        if (ls * ms > 0.0f) {
-          l = m, ls = ms, side |= 1 << k;
-        } else {
-          r = m, rs_ = ms;
-        }
-      }
-      if (found && fabsf(prev_sdf - s) < p.sample_sdf_threshold && fabsf(s) < p.sdf_threshold) {
-        tr.hit = true, tr.t0 = prev_t, tr.t1 = t, tr.side = side;
-        return tr;
-      }
-    }
-    prev_sdf = s, prev_t = t, have_prev = true;
-    t += step;
-  }
-  return tr;
-}
 
 __device__ __forceinline__ F3 cross3(F3 a, F3 b) {
   return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
@@ -598,33 +705,22 @@ __global__ void __launch_bounds__(RC_TX *RC_TY) k_raycast_grad(Dev d, int mode, 
       want = o > 0.0f && o < 1e30f;
     }
     if (want) {
-      RayCache c;
-      c.init();
-      const RayTrace tr = ray_trace(d, c, cam, wd, t_min, t_max);
-      if (tr.hit) {
+      // the forward's march: mode 1 takes its hit point and the alignment
+      // normal, taken 2.5 voxels either side (inside the truncation band):
+      // the half-voxel normal of the rendered image follows the noise of the
+      // fused surface, and a noisy normal in J shrinks every Gauss-Newton
+      // step (measured: from 2-8 cm / 1-2.5 degree starts, 8 iterations
+      // reached 15-90 mm with the half-voxel normal and 1-3 mm on three of
+      // four with this one)
+      const float spacing = mode == 1 ? fminf(2.5f, 0.8f * p.truncation_distance / p.voxel_size) : 0.0f;
+      const March mr = ray_march(d, cam, wd, t_min, t_max, spacing);
+      if (mr.hit) {
         if (mode == 1) {
-          // the forward's hit and normal
-          float l = tr.t0, r = tr.t1, ls, rs_, m = 0.0f;
-          ray_sample(d, c, f3(cam.x + l * wd.x, cam.y + l * wd.y, cam.z + l * wd.z), ls);
-          ray_sample(d, c, f3(cam.x + r * wd.x, cam.y + r * wd.y, cam.z + r * wd.z), rs_);
-          for (int k = 0; k < 3; ++k) {
-            m = l + (ls / (ls - rs_)) * (r - l);
-            float ms;
-            ray_sample(d, c, f3(cam.x + m * wd.x, cam.y + m * wd.y, cam.z + m * wd.z), ms);
-            if ((tr.side >> k) & 1) l = m, ls = ms;
-            else r = m, rs_ = ms;
-          }
+          const float m = mr.m;
           const float o = obs[pix];
           const F3 pm = f3(cam.x + m * wd.x, cam.y + m * wd.y, cam.z + m * wd.z);
-          // the normal of the alignment is taken 2.5 voxels either side
-          // (inside the truncation band): the half-voxel normal of the
-          // rendered image follows the noise of the fused surface, and a
-          // noisy normal in J shrinks every Gauss-Newton step (measured: from
-          // 2-8 cm / 1-2.5 degree starts, 8 iterations reached 15-90 mm with
-          // the half-voxel normal and 1-3 mm on three of four with this one)
-          const float spacing = fminf(2.5f, 0.8f * p.truncation_distance / p.voxel_size);
-          F3 g;
-          if (fabsf(m * cd.z - o) < max_res && ray_gradient(d, c, pm, g, spacing)) {
+          const F3 g = mr.g;
+          if (fabsf(m * cd.z - o) < max_res && mr.g_ok) {
             const float gl = sqrtf(dot3(g, g));
             if (gl > 0.0f) {
               // projective point-to-plane: the observed point on the same ray
@@ -639,6 +735,11 @@ __global__ void __launch_bounds__(RC_TX *RC_TY) k_raycast_grad(Dev d, int mode, 
             }
           }
         } else {
+          // the adjoints re-evaluate the bracketing samples and the three
+          // regula-falsi steps along the march's decisions
+          RayCache c;
+          c.init();
+          const RayTrace tr{true, mr.t0, mr.t1, mr.side};
           used = pixel_backward(d, c, cTw, cam, wd, cd.z, tr, aD, aN, dLdN != nullptr, grad, av, aw);
         }
       }

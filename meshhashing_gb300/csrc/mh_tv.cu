@@ -10,14 +10,14 @@
 // boundaries and stay invalid), tau = sigma = 1/sqrt(8).
 //
 // Two forms, bit-identical to each other:
-//  * k_tv_iter, one launch per iteration (the batch twin and the
-//    allocation-free entry point): each thread recomputes the dual update of
-//    its own pixel and of its left and upper neighbours (the ones its
-//    divergence needs) from the previous iterate, so the dual and primal
-//    steps fuse into a single pass with no grid-wide barrier;
-//  * k_tv_tile (a volume's frames): ten iterations per launch on a 64 x 32
-//    tile held in shared memory with a 10-pixel halo, so 20 iterations take
-//    2 launches instead of 22.
+//  * k_tv_iter, one launch per iteration (the allocation-free entry point):
+//    each thread recomputes the dual update of its own pixel and of its left
+//    and upper neighbours (the ones its divergence needs) from the previous
+//    iterate, so the dual and primal steps fuse into a single pass with no
+//    grid-wide barrier;
+//  * k_tv_tile (a volume's frames) and its batch twin k_tv_tile_b: ten
+//    iterations per launch on a 64 x 32 tile held in shared memory with a
+//    10-pixel halo, so 20 iterations take 2 launches instead of 22.
 #include "mh_internal.cuh"
 #include "mh_kernels.h"
 #include "mh_batch.cuh"
@@ -65,12 +65,6 @@ __device__ __forceinline__ void tv_init_body(const float *depth, float *f, float
   }
 }
 __global__ void k_tv_init(const float *depth, float *f, float *u, float *ub, float *px, float *py, int n) { tv_init_body(depth, f, u, ub, px, py, n); }
-__global__ void k_tv_init_b(const Scene *t, int n) {
-  each_scene(t, n, [&](const Scene &c) {
-    const size_t np = (size_t)c.d.p.width * c.d.p.height;
-    tv_init_body(c.d.depth, c.tv, c.tv + np, c.tv + 2 * np, c.tv + 3 * np, c.tv + 4 * np, (int)np);
-  });
-}
 
 __device__ __forceinline__ void tv_iter_body(const TvBuf &b) {
   const float tau = 0.35355339059327373f, sigma = 0.35355339059327373f;
@@ -97,30 +91,18 @@ __device__ __forceinline__ void tv_iter_body(const TvBuf &b) {
   }
 }
 __global__ void __launch_bounds__(256) k_tv_iter(TvBuf b) { tv_iter_body(b); }
-// iteration `it` of a batch: planes 1-4 hold the iterate after an even number
-// of iterations, planes 5-8 after an odd number
-__global__ void __launch_bounds__(256) k_tv_iter_b(const Scene *t, int n, int it, float lambda) {
-  each_scene(t, n, [&](const Scene &c) {
-    const size_t np = (size_t)c.d.p.width * c.d.p.height;
-    float *A = c.tv + np * ((it & 1) ? 5 : 1), *B = c.tv + np * ((it & 1) ? 1 : 5);
-    TvBuf b;
-    b.f = c.tv;
-    b.u = A, b.ub = A + np, b.px = A + 2 * np, b.py = A + 3 * np;
-    b.u2 = B, b.ub2 = B + np, b.px2 = B + 2 * np, b.py2 = B + 3 * np;
-    b.W = c.d.p.width, b.H = c.d.p.height, b.lambda = lambda;
-    tv_iter_body(b);
-  });
-}
 
 __device__ __forceinline__ void tv_out_body(const float *f, const float *u, float *depth, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     depth[i] = valid_at(f, i) ? u[i] * 0.001f : -__int_as_float(0x7f800000);
 }
 __global__ void k_tv_out(const float *f, const float *u, float *depth, int n) { tv_out_body(f, u, depth, n); }
-__global__ void k_tv_out_b(const Scene *t, int n, int iterations) {
+// a batch's TV result after `launches` tiled launches: planes 1-4 hold the
+// iterate after an even number of launches, planes 5-8 after an odd number
+__global__ void k_tv_out_b(const Scene *t, int n, int launches) {
   each_scene(t, n, [&](const Scene &c) {
     const size_t np = (size_t)c.d.p.width * c.d.p.height;
-    tv_out_body(c.tv, c.tv + np * ((iterations & 1) ? 5 : 1), c.d.depth, (int)np);
+    tv_out_body(c.tv, c.tv + np * ((launches & 1) ? 5 : 1), c.d.depth, (int)np);
   });
 }
 
@@ -153,11 +135,11 @@ struct TvTile {
   float lambda;
 };
 
-__global__ void __launch_bounds__(1024) k_tv_tile(TvTile b) {
+__device__ __forceinline__ void tv_tile_body(const TvTile &b, int tile_x, int tile_y) {
   extern __shared__ float sm[];
   float *sf = sm, *su = sm + TV_RN, *sub = sm + 2 * TV_RN, *spx = sm + 3 * TV_RN, *spy = sm + 4 * TV_RN;
   const float tau = 0.35355339059327373f, sigma = 0.35355339059327373f;
-  const int x0 = blockIdx.x * TV_TW - TV_K, y0 = blockIdx.y * TV_TH - TV_K;
+  const int x0 = tile_x * TV_TW - TV_K, y0 = tile_y * TV_TH - TV_K;
   const float NI = -__int_as_float(0x7f800000);
   for (int r = threadIdx.x; r < TV_RN; r += blockDim.x) {
     const int gx = x0 + r % TV_RW, gy = y0 + r / TV_RW;
@@ -220,6 +202,32 @@ __global__ void __launch_bounds__(1024) k_tv_tile(TvTile b) {
     }
   }
 }
+__global__ void __launch_bounds__(1024) k_tv_tile(TvTile b) { tv_tile_body(b, blockIdx.x, blockIdx.y); }
+
+int tv_tile_count(int W, int H) { return ((W + TV_TW - 1) / TV_TW) * ((H + TV_TH - 1) / TV_TH); }
+
+// Launch `launch` (of ceil(iterations / TV_K)) of the tiled TV for every
+// active scene: the scenes' tiles are concatenated (Scene::tv_tile0); planes
+// 1-4 of a scene's TV scratch hold the iterate after an even number of
+// launches, planes 5-8 after an odd number.  Bit-identical to the single
+// scene's launches, and so to one launch per iteration.
+__global__ void __launch_bounds__(1024) k_tv_tile_b(const Scene *t, int n, int total, int launch, int iters, int last,
+                                                    float lambda) {
+  each_tile(t, n, total, &Scene::tv_tile0, [&](const Scene &c, int lt) {
+    const int W = c.d.p.width, H = c.d.p.height;
+    const size_t np = (size_t)W * H;
+    float *A = c.tv + np * ((launch & 1) ? 5 : 1), *B = c.tv + np * ((launch & 1) ? 1 : 5);
+    TvTile b;
+    b.depth_in = launch == 0 ? c.d.depth : nullptr;
+    b.depth_out = (launch > 0 && last) ? c.d.depth : nullptr;
+    b.f = c.tv;
+    b.u = A, b.ub = A + np, b.px = A + 2 * np, b.py = A + 3 * np;
+    b.u2 = B, b.ub2 = B + np, b.px2 = B + 2 * np, b.py2 = B + 3 * np;
+    b.W = W, b.H = H, b.iters = iters, b.lambda = lambda;
+    const int tw = (W + TV_TW - 1) / TV_TW;
+    tv_tile_body(b, lt % tw, lt / tw);
+  });
+}
 
 int launch_denoise_tv_iterated(const Dev &d, float *tv, float lambda, int iterations, cudaStream_t s);
 
@@ -260,8 +268,8 @@ int launch_denoise_tv(const Dev &d, float *tv, float lambda, int iterations, cud
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }
 
-// the one-launch-per-iteration form (kept for reference timing; the batch
-// path runs its twin k_tv_iter_b)
+// the one-launch-per-iteration form (zero iterations, and the reference
+// timing of the tiled form)
 int launch_denoise_tv_iterated(const Dev &d, float *tv, float lambda, int iterations, cudaStream_t s) {
   const int W = d.p.width, H = d.p.height, n = W * H;
   const int g = min((n + 255) / 256, mh_sm_count() * 8);
@@ -355,11 +363,26 @@ extern "C" int mh_denoise_tv_static(const float *depth_in, float *depth_out, int
 }
 
 // ------------------------------------------------------------------ batched
-int launch_batch_tv(const Scene *t, int n, int max_pixels, float lambda, int iterations, cudaStream_t s) {
-  const int g = std::max(1, std::min((max_pixels + 255) / 256, mh_sm_count() * 8));
-  k_tv_init_b<<<g, 256, 0, s>>>(t, n);
-  for (int it = 0; it < iterations; ++it) k_tv_iter_b<<<g, 256, 0, s>>>(t, n, it, lambda);
-  k_tv_out_b<<<g, 256, 0, s>>>(t, n, iterations);
-  mh_count_launches(2 + iterations);
+// The batch's TV: the tiled kernel over all scenes' tiles, TV_K iterations
+// per launch (20 iterations: 2 launches instead of 22).
+int launch_batch_tv(const Scene *t, int n, int tv_tiles, float lambda, int iterations, cudaStream_t s) {
+  if (iterations <= 0 || tv_tiles <= 0) return MH_OK;
+  if (cudaFuncSetAttribute(k_tv_tile_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTvTileSmem) !=
+      cudaSuccess)
+    return MH_ERR_CUDA;
+  const int launches = (iterations + TV_K - 1) / TV_K;
+  const int g = std::max(1, std::min(tv_tiles, mh_sm_count() * 2));
+  for (int k = 0; k < launches; ++k) {
+    const int iters = std::min(TV_K, iterations - k * TV_K);
+    k_tv_tile_b<<<g, 1024, kTvTileSmem, s>>>(t, n, tv_tiles, k, iters, k == launches - 1 ? 1 : 0, lambda);
+  }
+  int count = launches;
+  if (launches == 1) {
+    // one launch reads the frame, so the result is written back separately
+    const int g2 = std::max(1, mh_sm_count() * 8);
+    k_tv_out_b<<<g2, 256, 0, s>>>(t, n, 1);
+    ++count;
+  }
+  mh_count_launches(count);
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }

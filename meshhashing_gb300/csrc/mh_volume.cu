@@ -128,13 +128,25 @@ __global__ void k_scatter_fields(Dev d, const int *ptr, int n, const float *sdf,
   if (blk >= n) return;
   const int p = ptr[blk];
   if (p < 0) return;
+  __shared__ int npos;
+  if (threadIdx.x == 0) npos = 0;
+  __syncthreads();
+  int mine = 0;
   for (int v = threadIdx.x; v < MH_BLOCK_VOXELS; v += blockDim.x) {
     const size_t src = (size_t)blk * MH_BLOCK_VOXELS + v, dst = (size_t)p * MH_BLOCK_VOXELS + v;
     if (v == 0) d.wmax[p] = __int_as_float(0x7f800000);
-    if (sdf) d.sdf[dst] = sdf[src];
+    if (sdf) {
+      d.sdf[dst] = sdf[src];
+      mine += sdf_positive(sdf[src]);
+    }
     if (w) d.w[dst] = w[src];
     if (a) d.a[dst] = a[src];
     if (b) d.b[dst] = b[src];
+  }
+  if (sdf) {
+    atomicAdd(&npos, mine);
+    __syncthreads();
+    if (threadIdx.x == 0) d.posc[p] = npos;
   }
 }
 
@@ -232,6 +244,7 @@ int mh_volume_reset(mh_volume *v, void *stream) {
   MH_CUDA_TRY(cudaMemsetAsync(d.boundary, 0, sizeof(int) * cap, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.nvtx, 0, sizeof(int) * cap, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.wmax, 0, sizeof(float) * cap, s));
+  MH_CUDA_TRY(cudaMemsetAsync(d.posc, 0, sizeof(int) * cap, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.page_of, 0xFF, sizeof(int) * cap, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.page_owner, 0xFF, sizeof(int) * (size_t)npg, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.cube, 0, pv, s));
@@ -338,6 +351,7 @@ int mh_volume_create(const mh_params *p, mh_volume **out) {
   const size_t pv = (size_t)d.page_capacity * MH_BLOCK_VOXELS;
   A(dalloc(v, &d.page_of, cap));
   A(dalloc(v, &d.wmax, cap));
+  A(dalloc(v, &d.posc, cap));
   A(dalloc(v, &d.mesh_list, cap));
   A(dalloc(v, &d.cube_list, cap));
   A(dalloc(v, &d.vtx_list, cap));
@@ -379,6 +393,7 @@ int mh_volume_destroy(mh_volume *v) {
   for (void *p : v->allocs) cudaFree(p);
   if (v->scratch) cudaFree(v->scratch);
   if (v->acc) cudaFree(v->acc);
+  if (v->touch) cudaFree(v->touch);
   mh_pd_free(v);
   delete v;
   return MH_OK;
@@ -528,6 +543,31 @@ int mh_raycast(mh_volume *v, const float cTw[16], float *depth, float *vertex4, 
   }
   MH_CUDA_TRY(cudaMemcpyAsync(v->d.fc, &fc, sizeof(FrameConst), cudaMemcpyHostToDevice, s));
   return raycast_impl(v, depth, vertex4, normal4, out_on_device, s);
+}
+
+int mh_raycast_footprint(mh_volume *v, const float cTw[16], int *blocks_touched, void *stream) {
+  CHECK_VOL(v);
+  if (!cTw || !blocks_touched) return MH_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int cap = v->d.p.value_capacity;
+  if (!v->touch) MH_CUDA_TRY(cudaMalloc(&v->touch, (size_t)cap + 16));
+  int *dcount = reinterpret_cast<int *>(v->touch + ((size_t)cap + 3) / 4 * 4);
+  MH_CUDA_TRY(cudaMemsetAsync(v->touch, 0, (size_t)cap + 16, s));
+  FrameConst &fc = v->fc_host;
+  memcpy(fc.rc_cTw, cTw, sizeof(float) * 16);
+  inverse4(fc.rc_cTw, fc.rc_wTc);
+  if (!v->has_frame) {
+    memcpy(fc.cTw, cTw, sizeof(float) * 16);
+    memcpy(fc.wTc, fc.rc_wTc, sizeof(float) * 16);
+  }
+  MH_CUDA_TRY(cudaMemcpyAsync(v->d.fc, &fc, sizeof(FrameConst), cudaMemcpyHostToDevice, s));
+  Dev d = v->d;
+  d.touch = v->touch;
+  TRY(launch_raycast(d, nullptr, nullptr, nullptr, s));
+  TRY(launch_count_flags(v->touch, cap, dcount, s));
+  MH_CUDA_TRY(cudaMemcpyAsync(blocks_touched, dcount, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MH_CUDA_TRY(cudaStreamSynchronize(s));
+  return MH_OK;
 }
 
 int mh_integrate_frame(mh_volume *v, const float *depth, int depth_on_device, const float wTc[16], int tv_iterations,
@@ -834,6 +874,18 @@ int mh_dump_block_meta(mh_volume *v, int n, const int32_t *pos, int32_t *life, i
       else MH_CUDA_TRY(cudaMemcpy(dst[f] + i, src[f] + p, sizeof(int), cudaMemcpyDeviceToHost));
     }
   }
+  return MH_OK;
+}
+
+int mh_dump_positive_counts(mh_volume *v, int n, const int32_t *pos, int32_t *count) {
+  CHECK_VOL(v);
+  if (n < 0 || (n > 0 && (!pos || !count))) return MH_ERR_INVALID;
+  MH_CUDA_TRY(cudaDeviceSynchronize());
+  std::vector<int> ptr;
+  TRY(find_ptrs(v, n, pos, ptr, false));
+  std::vector<int> all((size_t)v->d.p.value_capacity);
+  MH_CUDA_TRY(cudaMemcpy(all.data(), v->d.posc, sizeof(int) * all.size(), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; ++i) count[i] = ptr[i] < 0 ? INT32_MIN : all[ptr[i]];
   return MH_OK;
 }
 

@@ -16,6 +16,7 @@ struct mh_volume {
   float *tv = nullptr;
   float *rc_stage = nullptr;  // device staging for host raycast outputs
   double *acc = nullptr;      // reduction target of the raycast gradients (allocated on first use)
+  uint8_t *touch = nullptr;   // raycast footprint flags, one per block (allocated on first use)
   mh_pd_state *pd = nullptr;  // Huber-TV state (allocated on first use)
   int *scratch = nullptr;     // device scratch for list operations
   size_t scratch_bytes = 0;

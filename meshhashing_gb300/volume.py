@@ -166,6 +166,14 @@ class Volume:
         self._c("mh_raycast", _ptr(m), _dev(depth_out), _dev(vertex_out), _dev(normal_out), 1, self.stream)
         return None
 
+    def raycast_footprint(self, cTw) -> int:
+        """Distinct blocks the raycast from cTw looks up and finds (its block
+        footprint); the outputs are discarded."""
+        m = _f32(cTw).reshape(16)
+        n = C.c_int32(0)
+        self._c("mh_raycast_footprint", _ptr(m), C.byref(n), self.stream)
+        return n.value
+
     # ---------------------------------------------------------- mesh export
     def compact_mesh(self):
         """(positions (V, 3), normals (V, 3), triangles (T, 3) int32): the
@@ -361,6 +369,13 @@ class Volume:
         self._c("mh_dump_block_meta", n, _ptr(pos, C.c_int32), _ptr(life, C.c_int32), _ptr(inner, C.c_int32),
                 _ptr(bnd, C.c_int32))
         return life, inner, bnd
+
+    def positive_counts(self, pos):
+        """Per block: the library's count of voxels with sdf in (1e-30, 1e30)."""
+        pos = _i32(pos).reshape(-1, 3)
+        out = np.zeros(len(pos), np.int32)
+        self._c("mh_dump_positive_counts", len(pos), _ptr(pos, C.c_int32), _ptr(out, C.c_int32))
+        return out
 
     def flags(self):
         n = C.c_int32(0)
