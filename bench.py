@@ -172,6 +172,8 @@ def bytes_per_launch(stage, nb, px, rpx, vwork, cube_blocks=0, mesh_blocks=0, pr
 # ---------------------------------------------------------------- batched scenes
 BATCH_RES = ((160, 120), (320, 240), (640, 480))
 BATCH_VOXEL = (0.004, 0.006, 0.008)
+BATCH_BLOCKS_PER_PIXEL = 0.075   # pool growth per pixel per frame (to be replaced by the measured rate)
+BATCH_SWEPT_M3 = 1e9
 
 
 def batch_specs(n_scenes):
@@ -193,28 +195,37 @@ def _batch_frame_job(args):
     return wl.frame(i), wl.pose(i)
 
 
-def gen_batch_frames(specs, n):
+def gen_batch_frames(specs):
+    """Every frame of every scene's own sequence (spec["frames"] frames)."""
     ctx = mp.get_context("spawn")
-    jobs = [(sp, i) for sp in specs for i in range(n)]
+    jobs = [(sp, i) for sp in specs for i in range(sp["frames"])]
     with ctx.Pool(min(os.cpu_count() or 4, 16)) as pool:
-        out = pool.map(_batch_frame_job, jobs, chunksize=4)
-    frames = [[out[k * n + i][0] for i in range(n)] for k in range(len(specs))]
-    poses = [[out[k * n + i][1] for i in range(n)] for k in range(len(specs))]
+        out = pool.map(_batch_frame_job, jobs, chunksize=8)
+    frames, poses, k = [], [], 0
+    for sp in specs:
+        frames.append([out[k + i][0] for i in range(sp["frames"])])
+        poses.append([out[k + i][1] for i in range(sp["frames"])])
+        k += sp["frames"]
     return frames, poses
 
 
-def batch_params(spec, frames_run):
-    """Pools sized for frames_run frames of the outlier-heavy stream: ~7.5 % of
-    the pixels allocate a block per frame (5 % outliers) plus the surface."""
+def batch_params(spec):
+    """Pools sized for the scene's whole sequence: BATCH_BLOCKS_PER_PIXEL
+    blocks per pixel per frame (measured growth of these scenes, dominated
+    by the 5 % outliers, with margin) plus a surface allowance, capped by the
+    room's swept volume at the voxel size."""
     from meshhashing_gb300 import config, scene
     wl = scene.full_spline(spec["frames"], seed=spec["seed"], width=spec["width"], height=spec["height"])
     px = spec["width"] * spec["height"]
-    cap = int(px * (0.075 * frames_run + 0.6) * 1.4) // 1024 * 1024 + 1024
+    vox = spec["voxel"]
+    grow = int(px * (BATCH_BLOCKS_PER_PIXEL * spec["frames"] + 0.6))
+    swept = int(BATCH_SWEPT_M3 / (8 * vox) ** 3)
+    cap = min(grow, swept) // 1024 * 1024 + 4096
     buckets = 1 << max(14, (cap - 1).bit_length())
     pools = 1 << max(15, (cap // 2 - 1).bit_length())
-    return config.params_for(wl, voxel_size=spec["voxel"], truncation=3 * spec["voxel"], value_capacity=cap,
+    return config.params_for(wl, voxel_size=vox, truncation=3 * vox, value_capacity=cap,
                              bucket_count=buckets, max_vertex_count=pools, max_triangle_count=pools,
-                             overflow_capacity=max(buckets // 4, 1024), mesh_page_capacity=max(cap // 64, 2048))
+                             overflow_capacity=max(buckets // 4, 1024), mesh_page_capacity=max(cap // 32, 2048))
 
 
 def run_pose_refinement(params, frames, poses, W, H, fused=100, refined=200, iterations=10):
@@ -323,80 +334,101 @@ def run_huber_tv(vol, peak, iterations=10):
             "note": "CUDA events around the iterations; the energy read-back at the end is inside the timing"}
 
 
-def run_batched(specs, frames, poses, P, W, K):
-    """Aggregate frames/s of the scenes advanced one after another with the
-    plain per-frame chain, then (same volumes, reset) as one batch: one launch
-    per stage for all scenes, autotuned during the P pre-fuse steps, the step
+def run_batched(specs, frames, poses):
+    """The batched-fusion schedule: every scene advances through its own
+    frame count (U[20, 200]); aggregate frames/s over the whole schedule,
+    first with the scenes one after another through the plain per-frame
+    chain, then (same volumes, reset) as one batch: one launch per stage for
+    all scenes still running (scenes whose sequence ended are retired through
+    the step's active mask), autotuned on a separate pass, every step
     replayed from a CUDA graph."""
     import torch
     from meshhashing_gb300 import Batch, Volume
     n = len(specs)
-    vols = [Volume(batch_params(sp, P + W + K)) for sp in specs]
+    nfr = [sp["frames"] for sp in specs]
+    total_frames = int(sum(nfr))
+    steps = max(nfr)
+    vols = [Volume(batch_params(sp)) for sp in specs]
     dev = [torch.from_numpy(np.stack(f)).cuda() for f in frames]
     outs = [torch.empty((sp["height"], sp["width"]), dtype=torch.float32, device="cuda") for sp in specs]
-
-    def plain(i):
-        for s in range(n):
-            vols[s].integrate_frame(dev[s][i], poses[s][i], on_device=True, tv_iterations=TV_ITERS,
-                                    tv_lambda=TV_LAMBDA, ray_depth=outs[s], outputs_on_device=True)
-
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for i in range(P + W):
-        plain(i)
+
+    def plain_frame(s, i):
+        vols[s].integrate_frame(dev[s][i], poses[s][i], on_device=True, tv_iterations=TV_ITERS,
+                                tv_lambda=TV_LAMBDA, ray_depth=outs[s], outputs_on_device=True)
+
+    # warm-up: three frames of every scene, then every volume starts empty
+    for s in range(n):
+        for i in range(3):
+            plain_frame(s, i)
     torch.cuda.synchronize()
+    for v in vols:
+        v.reset()
     e0.record()
-    for i in range(P + W, P + W + K):
-        plain(i)
+    for s in range(n):
+        for i in range(nfr[s]):
+            plain_frame(s, i)
     e1.record()
     torch.cuda.synchronize()
     plain_ms = e0.elapsed_time(e1)
     err_plain = sum(v.stats()["error"] != 0 for v in vols)
+    plain_blocks = [v.stats()["blocks_allocated"] for v in vols]
+
+    batch = Batch(vols, raycast=True)
     for v in vols:
         v.reset()
-    batch = Batch(vols, raycast=True)
-    batch.autotune(max(1, P // 9))
+    tune_steps = 9
+    batch.autotune(1)
 
     def bstep(i, graph):
-        batch.step([dev[s][i] for s in range(n)], [poses[s][i] for s in range(n)], on_device=True,
-                   tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA, use_graph=graph)
+        act = [i < nfr[s] for s in range(n)]
+        batch.step([dev[s][i] if act[s] else None for s in range(n)], [poses[s][i] if act[s] else None for s in range(n)],
+                   active=act, on_device=True, tv_iterations=TV_ITERS, tv_lambda=TV_LAMBDA, use_graph=graph)
 
-    for i in range(P):
+    # autotuning and graph capture on a pass over the first steps, then every
+    # volume starts empty again
+    for i in range(tune_steps):
         bstep(i, False)
-    for i in range(P, P + W):
+    for i in range(tune_steps, tune_steps + 2):
         bstep(i, True)
     torch.cuda.synchronize()
+    tuning, times, stage = batch.tuning(), batch.tuning_times(), batch.stage_times()
+    for v in vols:
+        v.reset()
     e0.record()
-    for i in range(P + W, P + W + K):
+    for i in range(steps):
         bstep(i, True)
     e1.record()
     torch.cuda.synchronize()
     batch_ms = e0.elapsed_time(e1)
     err_batch = sum(v.stats()["error"] != 0 for v in vols)
-    tuning, times, stage = batch.tuning(), batch.tuning_times(), batch.stage_times()
+    same_blocks = all(v.stats()["blocks_allocated"] == b for v, b in zip(vols, plain_blocks))
     batch.close()
     for v in vols:
         v.close()
-    res = {}
+    del dev
+    res, vox = {}, {}
     for sp in specs:
         k = "%dx%d" % (sp["width"], sp["height"])
         res[k] = res.get(k, 0) + 1
-    vox = {}
-    for sp in specs:
         k = "%d" % round(sp["voxel"] * 1000)
         vox[k] = vox.get(k, 0) + 1
-    frames_per_step = n
-    return {"workload": "%d independent room scenes (seeds 0..%d), PSDF, TV %d it, raycast" % (n, n - 1, TV_ITERS),
-            "scenes": n, "resolutions": res, "voxel_mm": vox, "steps": K, "warmup": W, "prefuse": P,
-            "value": frames_per_step * K / (batch_ms / 1000.0), "unit": "frames/s (all scenes)",
-            "plain_value": frames_per_step * K / (plain_ms / 1000.0),
-            "speedup_vs_plain": plain_ms / batch_ms, "ms_per_step": batch_ms / K, "plain_ms_per_step": plain_ms / K,
-            "form": "one launch per stage for all scenes, step replayed from a CUDA graph",
-            "plain_form": "scenes one after another, per-frame stream launches",
+    return {"workload": "%d independent room scenes (seeds 0..%d), frame counts U[20, 200], PSDF, TV %d it, raycast"
+                        % (n, n - 1, TV_ITERS),
+            "scenes": n, "resolutions": res, "voxel_mm": vox, "frames_total": total_frames, "steps": steps,
+            "value": total_frames / (batch_ms / 1000.0), "unit": "frames/s (all scenes)",
+            "plain_value": total_frames / (plain_ms / 1000.0),
+            "speedup_vs_plain": plain_ms / batch_ms, "batch_s": batch_ms / 1000.0, "plain_s": plain_ms / 1000.0,
+            "form": "one launch per stage for the scenes still running (active mask), each step replayed from a "
+                    "CUDA graph",
+            "plain_form": "scenes one after another, each through its whole sequence, per-frame stream launches",
+            "same_block_counts": bool(same_blocks),
             "tuning": {"chosen": {"ray_tile": list(tuning["ray_tile"]),
                                   "integrate_cta_per_sm": tuning["integrate_cta_per_sm"]},
                        "raycast_ms": {"%dx%d" % k: v for k, v in times["raycast_ms"].items()},
-                       "integrate_ms": {str(k): v for k, v in times["integrate_ms"].items()}},
-            "stage_ms_per_step": stage,
+                       "integrate_ms": {str(k): v for k, v in times["integrate_ms"].items()},
+                       "stage_ms_per_step": stage,
+                       "note": "autotuning steps 0..8 of the schedule on a separate pass (small maps)"},
             "scenes_with_error": {"plain": int(err_plain), "batched": int(err_batch)}}
 
 
@@ -561,7 +593,6 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=64,
                     help="scenes of the batched-vs-plain measurement (0: skip it)")
-    ap.add_argument("--batch-steps", type=int, default=5)
     ap.add_argument("--stream-frames", type=int, default=STREAM_FRAMES,
                     help="frames of the floor-plan streaming measurement (0: skip it)")
     ap.add_argument("--pose-refined", type=int, default=POSE_REFINED,
@@ -594,8 +625,7 @@ def main():
         cpu_frames = (frames[:args.cpu_frames], poses[:args.cpu_frames])
 
     bspecs = batch_specs(args.batch_scenes) if (args.batch_scenes > 0 and world == 1) else []
-    BP, BW, BK = 9, 3, args.batch_steps
-    bframes = gen_batch_frames(bspecs, BP + BW + BK) if bspecs else None
+    bframes = gen_batch_frames(bspecs) if bspecs else None
     sframes = gen_stream_frames(args.stream_frames) if (args.stream_frames > 0 and world == 1) else None
 
     import torch
@@ -712,10 +742,10 @@ def main():
         if args.pose_refined > 0 else None
     batched = None
     if bspecs:
-        batched = run_batched(bspecs, bframes[0], bframes[1], BP, BW, BK)
+        batched = run_batched(bspecs, bframes[0], bframes[1])
         small = [k for k, sp in enumerate(bspecs) if sp["width"] < 640]
         batched["below_640x480"] = run_batched([bspecs[k] for k in small], [bframes[0][k] for k in small],
-                                               [bframes[1][k] for k in small], BP, BW, BK)
+                                               [bframes[1][k] for k in small])
     stream = run_stream(*sframes) if sframes else None
 
     cpu = None
