@@ -84,6 +84,7 @@ def lib():
         L.ref_dump_mesh.argtypes = [vp, C.c_int, i32p, f32p, C.c_int, i32p, i32p, i32p]
         L.ref_inverse.argtypes = [f32p, f32p]
         L.ref_cube_indices.argtypes = [vp, C.c_int, i32p, C.POINTER(C.c_uint8)]
+        L.ref_compress_mesh.argtypes = [vp, C.c_int, f32p, f32p, C.c_int, i32p, i32p]
         L.ref_pd_init.argtypes = [vp]
         L.ref_point_to_psdf.argtypes = [vp, f32p, f32p, f32p, f32p, i32p]
         L.ref_set_candidates.restype = C.c_int
@@ -203,6 +204,19 @@ class RefCPU:
         self.L.ref_dump_mesh(self.h, a, _p(vk, C.c_int32), _p(vd, C.c_float), b, _p(tr, C.c_int32),
                              C.byref(nv), C.byref(nt))
         return vk[:a], vd[:a], tr[:b]
+
+    def compress_mesh(self):
+        """MainEngine's compact mesh (CollectAllBlocks + CompressMesh):
+        (positions[nv, 3], normals[nv, 3], triangles[nt, 3], stats (nt, nv,
+        sum of the compacted vertices' ref_count))."""
+        st = np.zeros(3, np.int32)
+        self.L.ref_compress_mesh(self.h, 0, None, None, 0, None, _p(st, C.c_int32))
+        nt, nv = int(st[0]), int(st[1])
+        pos, nrm = np.zeros((max(nv, 1), 3), np.float32), np.zeros((max(nv, 1), 3), np.float32)
+        tri = np.zeros((max(nt, 1), 3), np.int32)
+        self.L.ref_compress_mesh(self.h, nv, _p(pos, C.c_float), _p(nrm, C.c_float), nt, _p(tri, C.c_int32),
+                                 _p(st, C.c_int32))
+        return pos[:nv], nrm[:nv], tri[:nt], st.copy()
 
     def cubes(self, pos):
         pos = np.ascontiguousarray(pos, np.int32).reshape(-1, 3)

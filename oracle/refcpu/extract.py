@@ -25,6 +25,7 @@ SOURCES = [
     ("src/mapping/recycle.cu", ()),
     ("src/optimize/primal_dual.cu", ()),
     ("src/localizing/point_to_psdf.cu", ()),
+    ("src/visualization/compress_mesh.cu", ()),
 ]
 
 

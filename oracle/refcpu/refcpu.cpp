@@ -34,6 +34,7 @@
 #include "geometry/primal_dual_query.h"
 #include "visualization/color_util.h"
 #include "meshing/mc_tables.h"
+#include "visualization/compact_mesh.h"
 
 #include <functional>
 #include <unordered_map>
@@ -279,6 +280,49 @@ void Mesh::Reset() {
   }
 }
 uint Mesh::vertex_heap_count() { return vertex_heap_counter_[0]; }
+
+// CompactMesh (visualization/compact_mesh.cu:16-95) in host memory
+void CompactMesh::Alloc(const MeshParams &mp) {
+  if (is_allocated_on_gpu_) return;
+  vertex_remapper_ = new int[mp.max_vertex_count];
+  vertex_counter_ = new uint[1];
+  vertices_ref_count_ = new int[mp.max_vertex_count];
+  vertices_ = new float3[mp.max_vertex_count];
+  normals_ = new float3[mp.max_vertex_count];
+  colors_ = new float3[mp.max_vertex_count];
+  triangle_counter_ = new uint[1];
+  triangles_ref_count_ = new int[mp.max_triangle_count];
+  triangles_ = new int3[mp.max_triangle_count];
+  is_allocated_on_gpu_ = true;
+}
+void CompactMesh::Free() {
+  if (!is_allocated_on_gpu_) return;
+  delete[] vertex_remapper_;
+  delete[] vertex_counter_;
+  delete[] vertices_ref_count_;
+  delete[] vertices_;
+  delete[] normals_;
+  delete[] colors_;
+  delete[] triangle_counter_;
+  delete[] triangles_ref_count_;
+  delete[] triangles_;
+  is_allocated_on_gpu_ = false;
+}
+void CompactMesh::Resize(const MeshParams &mp) {
+  mesh_params_ = mp;
+  Free();
+  Alloc(mp);
+  Reset();
+}
+void CompactMesh::Reset() {
+  std::memset(vertex_remapper_, 0xff, sizeof(int) * mesh_params_.max_vertex_count);
+  std::memset(vertices_ref_count_, 0, sizeof(int) * mesh_params_.max_vertex_count);
+  vertex_counter_[0] = 0;
+  std::memset(triangles_ref_count_, 0, sizeof(int) * mesh_params_.max_triangle_count);
+  triangle_counter_[0] = 0;
+}
+uint CompactMesh::vertex_count() { return vertex_counter_[0]; }
+uint CompactMesh::triangle_count() { return triangle_counter_[0]; }
 uint Mesh::triangle_heap_count() { return triangle_heap_counter_[0]; }
 
 // ------------------------------------------------------------------ driver
@@ -631,6 +675,42 @@ void ref_dump_mesh(void *h, int maxv, int32_t *vkeys, float *vdata, int maxt, in
   }
   *nv = v;
   *nt = t;
+}
+
+// MainEngine's mesh output (main_engine.cc:207-216): CollectAllBlocks
+// (core/collect_block_array.cu:97-117), then CompressMesh
+// (visualization/compress_mesh.cu:96-172) with the reference's launch
+// shapes.  Writes at most max_v compact vertices (pos3, normal3) and max_t
+// triangles (3 compact indices); stats = (triangles, vertices, sum of the
+// compacted vertices' ref_count).
+void ref_compress_mesh(void *h, int max_v, float *pos3, float *nrm3, int max_t, int32_t *tri3, int32_t *stats) {
+  Ref *r = (Ref *)h;
+  r->cand.reset_count();
+  launch(D3((r->hp.entry_count + 255) / 256), D3(256), true, [&] { CollectAllBlocksKernel(r->ht, r->cand); });
+  CompactMesh cm;
+  cm.Resize(r->mp);
+  int3 st = make_int3(0, 0, 0);
+  const uint n = r->cand.count();
+  if (n > 0) {
+    launch(D3(n), D3(BLOCK_SIZE), false, [&] { CollectVerticesAndTrianglesKernel(r->cand, r->blocks, r->mesh, cm); });
+    uint vref = 0;
+    launch(D3((r->mp.max_vertex_count + 255) / 256), D3(256), true,
+           [&] { CompressVerticesKernel(r->mesh, cm, r->mp.max_vertex_count, &vref); });
+    launch(D3((r->mp.max_triangle_count + 255) / 256), D3(256), true,
+           [&] { CompressTrianglesKernel(r->mesh, cm, r->mp.max_triangle_count); });
+    st = make_int3((int)cm.triangle_count(), (int)cm.vertex_count(), (int)vref);
+  }
+  stats[0] = st.x, stats[1] = st.y, stats[2] = st.z;
+  for (int i = 0; i < st.y && i < max_v; ++i) {
+    const float3 p = cm.vertices()[i], q = cm.normals()[i];
+    pos3[3 * i] = p.x, pos3[3 * i + 1] = p.y, pos3[3 * i + 2] = p.z;
+    nrm3[3 * i] = q.x, nrm3[3 * i + 1] = q.y, nrm3[3 * i + 2] = q.z;
+  }
+  for (int i = 0; i < st.x && i < max_t; ++i) {
+    const int3 t = cm.triangles()[i];
+    tri3[3 * i] = t.x, tri3[3 * i + 1] = t.y, tri3[3 * i + 2] = t.z;
+  }
+  cm.Free();
 }
 
 void ref_cube_indices(void *h, int n, const int32_t *pos, uint8_t *out) {

@@ -23,6 +23,12 @@ committed, so tests never need the tree.
   track_room96.npz   PointToSurface (localizing/point_to_psdf.cu) on the
                      simple chain's map with frame 18's depth at two poses
                      off the true one: A, b, err and count
+  compress_room96.npz MainEngine's mesh output on the simple chain's map:
+                     CollectAllBlocks + CompressMesh
+                     (visualization/compress_mesh.cu): compact vertex
+                     positions and normals, triangles as compact indices,
+                     and CompressMesh's stats (triangles, vertices, summed
+                     vertex reference counts)
 
 Both use params.compat_arithmetic = 1 (the reference's single-precision
 formulas as written).  Allocation is repeated until no block is added, which
@@ -187,6 +193,19 @@ def run_track(ref_mod, p, depth, poses):
                 err=np.array(out["err"], np.float32), count=np.array(out["count"], np.int32))
 
 
+def run_compress(ref_mod, p, depth, poses):
+    r = ref_mod.RefCPU(p)
+    for d, T in zip(depth, poses):
+        r.frame_set(d, T)
+        r.alloc(True)
+        r.collect()
+        r.integrate_simple()
+        r.mesh()
+        r.gc_low_surfel()
+    pos, nrm, tri, stats = r.compress_mesh()
+    return dict(depth=depth, poses=poses, pos=pos, normal=nrm, tris=tri, stats=stats)
+
+
 def rows(pos, field, want):
     idx = {tuple(q): i for i, q in enumerate(pos.tolist())}
     return np.stack([field[idx[tuple(q)]] for q in np.asarray(want).tolist()])
@@ -203,7 +222,8 @@ def main():
     p, depth, poses = simple_case()
     np.savez_compressed(os.path.join(HERE, "huber_room96.npz"), **run_huber(refcpu, p, depth, poses))
     np.savez_compressed(os.path.join(HERE, "track_room96.npz"), **run_track(refcpu, p, depth, poses))
-    for f in ("simple_room96.npz", "psdf_room96.npz", "huber_room96.npz", "track_room96.npz"):
+    np.savez_compressed(os.path.join(HERE, "compress_room96.npz"), **run_compress(refcpu, p, depth, poses))
+    for f in ("simple_room96.npz", "psdf_room96.npz", "huber_room96.npz", "track_room96.npz", "compress_room96.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

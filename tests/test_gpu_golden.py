@@ -18,6 +18,11 @@ def test_gpu_matches_reference_simple_chain(built):
     assert ntri > 500
 
 
+def test_gpu_matches_reference_compress_mesh(built):
+    nt, close = _golden.check_compress(_golden.GpuRunner)
+    assert nt > 10000
+
+
 def test_gpu_matches_reference_psdf_chain(built):
     _golden.check_psdf(_golden.GpuRunner)
 

@@ -64,3 +64,28 @@ def test_compact_matches_pools_and_ply(built, tmp_path):
     nl = np.array([[float(x) for x in ln.split()[1:]] for ln in lines if ln.startswith("vn ")], np.float32)
     fl = np.array([[int(x.split("//")[0]) for x in ln.split()[1:]] for ln in lines if ln.startswith("f ")])
     assert np.array_equal(vl, pos) and np.array_equal(nl, nrm) and np.array_equal(fl - 1, tri)
+
+
+def test_compact_matches_oracle_mesh(built):
+    """The dense mesh of a 30-frame map against the FP32 oracle's mesh of the
+    same frames (its MainEngine loop from the same empty volume): the same
+    triangles as triples of vertex-position bits, with multiplicity, and
+    the same vertex count."""
+    from collections import Counter
+    from oracle.oracle import Oracle
+    wl = scene.small_circle(60)
+    f = 262.5 * 160 / 320
+    wl.camera = scene.Camera(160, 120, f, f, 79.5, 59.5)
+    p = config.params_for(wl, value_capacity=1 << 16, bucket_count=1 << 15, max_vertex_count=1 << 18,
+                          max_triangle_count=1 << 18)
+    v = Volume(p)
+    o = Oracle(p, fp64=False)
+    for i in range(0, 60, 2):
+        v.integrate_frame(wl.frame(i), wl.pose(i))
+        o.frame(wl.frame(i), wl.pose(i))
+    pos, _, tri = v.compact_mesh()
+    vk, vd, tr = o.dump_mesh()
+    got = Counter(_tri_key(*[pos[k].view(np.uint32) for k in t]) for t in tri)
+    want = Counter(_tri_key(*[vd[int(k)][:3].view(np.uint32) for k in t[4:7]]) for t in tr)
+    assert len(tri) > 1000 and got == want
+    assert len(pos) == len(np.unique(tr[:, 4:7].reshape(-1)))
