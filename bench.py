@@ -172,8 +172,6 @@ def bytes_per_launch(stage, nb, px, rpx, vwork, cube_blocks=0, mesh_blocks=0, pr
 # ---------------------------------------------------------------- batched scenes
 BATCH_RES = ((160, 120), (320, 240), (640, 480))
 BATCH_VOXEL = (0.004, 0.006, 0.008)
-BATCH_BLOCKS_PER_PIXEL = 0.075   # pool growth per pixel per frame (to be replaced by the measured rate)
-BATCH_SWEPT_M3 = 1e9
 
 
 def batch_specs(n_scenes):
@@ -209,23 +207,31 @@ def gen_batch_frames(specs):
     return frames, poses
 
 
+# Block pool growth of the batched-fusion scenes, measured by fusing every
+# scene through its whole sequence with a generous pool: the high-water block
+# count follows about K * frames^0.62 for each (width, voxel mm) -- the 5 %
+# outliers in [0.3, 5] m keep allocating free space until the swept volume
+# fills.  K is the largest ratio seen in each group.
+BATCH_GROWTH_EXP = 0.62
+BATCH_GROWTH_K = {(160, 4): 9044, (160, 6): 6803, (160, 8): 4440,
+                  (320, 4): 23822, (320, 6): 14067, (320, 8): 8878,
+                  (640, 4): 53108, (640, 6): 19511, (640, 8): 12138}
+
+
 def batch_params(spec):
-    """Pools sized for the scene's whole sequence: BATCH_BLOCKS_PER_PIXEL
-    blocks per pixel per frame (measured growth of these scenes, dominated
-    by the 5 % outliers, with margin) plus a surface allowance, capped by the
-    room's swept volume at the voxel size."""
+    """Pools sized for the scene's whole sequence: 1.3 x the measured growth
+    of its (resolution, voxel) group, mesh pages for a thirty-second of the
+    blocks, vertex and triangle pools above the largest counts seen (286 k /
+    550 k)."""
     from meshhashing_gb300 import config, scene
     wl = scene.full_spline(spec["frames"], seed=spec["seed"], width=spec["width"], height=spec["height"])
-    px = spec["width"] * spec["height"]
     vox = spec["voxel"]
-    grow = int(px * (BATCH_BLOCKS_PER_PIXEL * spec["frames"] + 0.6))
-    swept = int(BATCH_SWEPT_M3 / (8 * vox) ** 3)
-    cap = min(grow, swept) // 1024 * 1024 + 4096
+    k = BATCH_GROWTH_K[(spec["width"], round(vox * 1000))]
+    cap = int(1.3 * k * spec["frames"] ** BATCH_GROWTH_EXP) // 1024 * 1024 + 4096
     buckets = 1 << max(14, (cap - 1).bit_length())
-    pools = 1 << max(15, (cap // 2 - 1).bit_length())
     return config.params_for(wl, voxel_size=vox, truncation=3 * vox, value_capacity=cap,
-                             bucket_count=buckets, max_vertex_count=pools, max_triangle_count=pools,
-                             overflow_capacity=max(buckets // 4, 1024), mesh_page_capacity=max(cap // 32, 2048))
+                             bucket_count=buckets, max_vertex_count=1 << 19, max_triangle_count=1 << 20,
+                             overflow_capacity=max(buckets // 4, 1024), mesh_page_capacity=max(cap // 32, 6144))
 
 
 def run_pose_refinement(params, frames, poses, W, H, fused=100, refined=200, iterations=10):
