@@ -37,6 +37,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "640×480 frames/s (alloc+fuse+mesh+raycast) batched vs plain, %HBM peak"
+_T0 = time.time()
+
+
+def log(msg):
+    """Progress on stderr (seconds since start); the result line is stdout."""
+    sys.stderr.write(f"[bench {time.time() - _T0:7.1f} s] {msg}\n")
+    sys.stderr.flush()
 TV_ITERS, TV_LAMBDA = 20, 0.1
 
 
@@ -370,6 +377,7 @@ def run_batched(specs, frames, poses):
     torch.cuda.synchronize()
     for v in vols:
         v.reset()
+    log(f"  {n} scenes created and warmed up; plain schedule")
     e0.record()
     for s in range(n):
         for i in range(nfr[s]):
@@ -377,6 +385,7 @@ def run_batched(specs, frames, poses):
     e1.record()
     torch.cuda.synchronize()
     plain_ms = e0.elapsed_time(e1)
+    log(f"  plain schedule {plain_ms / 1000:.1f} s; batch tuning")
     err_plain = sum(v.stats()["error"] != 0 for v in vols)
     plain_blocks = [v.stats()["blocks_allocated"] for v in vols]
 
@@ -401,12 +410,14 @@ def run_batched(specs, frames, poses):
     tuning, times, stage = batch.tuning(), batch.tuning_times(), batch.stage_times()
     for v in vols:
         v.reset()
+    log("  batched schedule")
     e0.record()
     for i in range(steps):
         bstep(i, True)
     e1.record()
     torch.cuda.synchronize()
     batch_ms = e0.elapsed_time(e1)
+    log(f"  batched schedule {batch_ms / 1000:.1f} s")
     err_batch = sum(v.stats()["error"] != 0 for v in vols)
     same_blocks = all(v.stats()["blocks_allocated"] == b for v, b in zip(vols, plain_blocks))
     batch.close()
@@ -625,14 +636,20 @@ def main():
     n_total = SEQ_FRAMES
     # frames are rendered in a spawn pool before any CUDA call
     n_pose = POSE_FUSED + args.pose_refined if args.pose_refined > 0 else 0
+    log("rendering the PSDF sequence")
     frames, poses = gen_frames(list(range(max(P + W + K + K2 + K3, n_pose))), SEQ_FRAMES)
     cpu_frames = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu_frames = (frames[:args.cpu_frames], poses[:args.cpu_frames])
 
     bspecs = batch_specs(args.batch_scenes) if (args.batch_scenes > 0 and world == 1) else []
+    if bspecs:
+        log(f"rendering the batched-fusion scenes ({sum(sp['frames'] for sp in bspecs)} frames)")
     bframes = gen_batch_frames(bspecs) if bspecs else None
+    if args.stream_frames > 0 and world == 1:
+        log(f"rendering {args.stream_frames} floor-plan frames")
     sframes = gen_stream_frames(args.stream_frames) if (args.stream_frames > 0 and world == 1) else None
+    log("frames ready")
 
     import torch
     torch.cuda.set_device(local)
@@ -664,6 +681,7 @@ def main():
         torch.cuda.synchronize()
 
     sampler = ClockSampler()
+    log("map pre-fused; timed region")
     sampler.start()
     time.sleep(0.3)                     # nvidia-smi is sampling before the timed region starts
     barrier()
@@ -742,20 +760,27 @@ def main():
             gbs = b / ((t_ms / c) / 1000.0) / 1e9 if t_ms > 0 else None
             stages[k] = {"ms_per_frame": t_ms / K2, "gbs": gbs, "frac": (gbs / peak) if gbs else None}
 
+    log("Huber-TV")
     huber = run_huber_tv(vol, peak)
     vol.close()
+    log("pose refinement")
     pose = run_pose_refinement(params, frames, poses, Ww, Hh, POSE_FUSED, args.pose_refined) \
         if args.pose_refined > 0 else None
     batched = None
     if bspecs:
+        log("batched fusion, all scenes")
         batched = run_batched(bspecs, bframes[0], bframes[1])
+        log("batched fusion, scenes below 640x480")
         small = [k for k, sp in enumerate(bspecs) if sp["width"] < 640]
         batched["below_640x480"] = run_batched([bspecs[k] for k in small], [bframes[0][k] for k in small],
                                                [bframes[1][k] for k in small])
+    if sframes:
+        log("streaming")
     stream = run_stream(*sframes) if sframes else None
 
     cpu = None
     if cpu_frames is not None:
+        log("CPU baseline")
         fps, cores, dt = run_cpu_baseline(params, *cpu_frames)
         cpu = {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
                "sample": f"frames 0..{len(cpu_frames[0]) - 1} from an empty volume (FP64 oracle), {dt:.1f} s"}
@@ -783,6 +808,7 @@ def main():
                "stream": stream,
                "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
+        log("done")
     if world > 1:
         torch.distributed.destroy_process_group()
 
