@@ -260,10 +260,10 @@ int mh_dump_block_meta(mh_volume *v, int n, const int32_t *pos, int32_t *life,
                        int32_t *inner, int32_t *boundary);
 int mh_dump_flags(mh_volume *v, int max_n, uint8_t *flags, int *n_out);
 /* Introspection, no reference counterpart: per block (INT32_MIN if absent)
- * the count the library keeps of voxels whose sdf lies in (1e-30, 1e30);
- * every sdf writer maintains it, and the raycast skips the trilinear
- * gathers of samples whose corner blocks all count 512. */
-int mh_dump_positive_counts(mh_volume *v, int n, const int32_t *pos, int32_t *count);
+ * the count the library keeps of voxels whose sdf lies in [0, 1e30); every
+ * sdf writer maintains it, and the raycast skips the trilinear gathers of
+ * samples whose corner blocks all count 512. */
+int mh_dump_nonneg_counts(mh_volume *v, int n, const int32_t *pos, int32_t *count);
 
 /* Per-stage GPU time, measured with CUDA events recorded on each stage's
  * stream around its launches (the reference's per-stage Timer and logging,

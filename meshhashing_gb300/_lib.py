@@ -55,7 +55,7 @@ SIGNATURES = {
     "mh_dump_cubes": (i32, [MHV, i32, i32p, u8p]),
     "mh_dump_block_meta": (i32, [MHV, i32, i32p, i32p, i32p, i32p]),
     "mh_dump_flags": (i32, [MHV, i32, u8p, i32p]),
-    "mh_dump_positive_counts": (i32, [MHV, i32, i32p, i32p]),
+    "mh_dump_nonneg_counts": (i32, [MHV, i32, i32p, i32p]),
     "mh_raycast_footprint": (i32, [MHV, f32p, i32p, vp]),
     "mh_hash_bucket": (C.c_uint32, [C.c_int32, C.c_int32, C.c_int32, C.c_uint32]),
     "mh_bytes_model": (i32, [MHV, C.POINTER(C.c_double)]),

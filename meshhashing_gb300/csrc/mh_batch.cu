@@ -315,6 +315,7 @@ int mh_batch_step(mh_batch *b, const float *const *depth, int depth_on_device, c
     const bool act = !active || active[i];
     sc.d = v->d;
     sc.d.fc = d_fc + i;
+    sc.d.cellok = nullptr;  // the batched raycast runs without the per-block cell flags
     sc.tv = v->tv;
     sc.ray_depth = b->out_depth[i];
     sc.ray_vert = reinterpret_cast<float4 *>(b->out_vert[i]);

@@ -227,8 +227,8 @@ __global__ void __launch_bounds__(256) k_pd_primal(Dev d, PD pd, const int *nbt,
     s = (s + lam * tau * s0) / (1.0f + lam * tau);
     if (w > 2.0f) s = s0;
     d.sdf[g] = s;
-    const int dpos = sdf_positive(s) - sdf_positive(prev);
-    if (dpos) atomicAdd(d.posc + blk, dpos);
+    const int dpos = sdf_nonneg(s) - sdf_nonneg(prev);
+    if (dpos) atomicAdd(d.nnc + blk, dpos);
     pd.bar[g] = 2.0f * s - prev;
   }
 }

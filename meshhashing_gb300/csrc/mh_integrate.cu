@@ -102,14 +102,14 @@ __device__ __forceinline__ void integrate_simple_body(const Dev &d) {
       if (!act[k]) continue;
       const float s0 = get(S, k), w0 = get(W, k);
       const float s1 = (s0 * w0 + sdf_new[k] * w_new[k]) / (w0 + w_new[k]);
-      dpos += sdf_positive(s1) - sdf_positive(s0);
+      dpos += sdf_nonneg(s1) - sdf_nonneg(s0);
       put(S, k, s1);
       put(W, k, w0 + w_new[k]);
     }
     *reinterpret_cast<float4 *>(d.sdf + base) = S;
     *reinterpret_cast<float4 *>(d.w + base) = W;
     note_wmax(d, cb.w, fmaxf(fmaxf(W.x, W.y), fmaxf(W.z, W.w)));
-    note_posc(d, cb.w, dpos);
+    note_nnc(d, cb.w, dpos);
   }
 }
 __global__ void __launch_bounds__(128) k_integrate_simple(Dev d) { integrate_simple_body(d); }
@@ -157,7 +157,7 @@ __device__ __forceinline__ void integrate_psdf_body(const Dev &d) {
     float4 W = *reinterpret_cast<const float4 *>(d.w + base);
     float4 A = *reinterpret_cast<const float4 *>(d.a + base);
     float4 B = *reinterpret_cast<const float4 *>(d.b + base);
-    const int pos_before = sdf_positive(S.x) + sdf_positive(S.y) + sdf_positive(S.z) + sdf_positive(S.w);
+    const int pos_before = sdf_nonneg(S.x) + sdf_nonneg(S.y) + sdf_nonneg(S.z) + sdf_nonneg(S.w);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       if (!act[k]) continue;
@@ -239,7 +239,7 @@ __device__ __forceinline__ void integrate_psdf_body(const Dev &d) {
     *reinterpret_cast<float4 *>(d.a + base) = A;
     *reinterpret_cast<float4 *>(d.b + base) = B;
     note_wmax(d, cb.w, fmaxf(fmaxf(W.x, W.y), fmaxf(W.z, W.w)));
-    note_posc(d, cb.w, sdf_positive(S.x) + sdf_positive(S.y) + sdf_positive(S.z) + sdf_positive(S.w) - pos_before);
+    note_nnc(d, cb.w, sdf_nonneg(S.x) + sdf_nonneg(S.y) + sdf_nonneg(S.z) + sdf_nonneg(S.w) - pos_before);
   }
 }
 __global__ void __launch_bounds__(128) k_integrate_psdf(Dev d) { integrate_psdf_body(d); }

@@ -109,7 +109,8 @@ struct Dev {
   int *life, *inner, *boundary, *nvtx;  // per block
   int *page_of;            // per block: mesh page or -1
   float *wmax;             // per block: upper bound of the largest voxel weight
-  int *posc;               // per block: voxels whose sdf is positive (sdf_positive), 512 = all
+  int *nnc;                // per block: voxels whose sdf is non-negative (sdf_nonneg), 512 = all
+  uint8_t *cellok;         // per block, set before a raycast: it and its 7 upper neighbours count 512 (null: unused)
   uint8_t *touch;          // per block: set by the raycast when a ray looks it up (null: not recorded)
   int *vtx_slot;           // [pages * 512 * 3]
   int *tri_slot;           // [pages * 512 * 5]
@@ -180,19 +181,18 @@ __device__ __forceinline__ int hash_find(const Dev &d, int x, int y, int z) {
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31; }
 
-// A voxel counts as positive when its sdf lies in (1e-30, 1e30).  A trilinear
-// sample whose eight corners are all positive is then positive itself: its
-// largest weight is at least 1/2 * 1/2 * 1/2, so that term alone is at least
-// 1.25e-31 and no term is NaN.  Every kernel that writes sdf keeps the
-// per-block count of such voxels (posc) exact; the raycast skips the gathers
-// of samples in blocks whose count is 512.
-__device__ __forceinline__ int sdf_positive(float s) { return s > 1e-30f && s < 1e30f ? 1 : 0; }
-// add the lanes' changes of one block's positive count (all active lanes of
-// the warp update the same block)
-__device__ __forceinline__ void note_posc(const Dev &d, int blk, int delta) {
+// A voxel counts as non-negative when its sdf lies in [0, 1e30) (NaN does
+// not).  A trilinear sample whose eight corners are all non-negative is then
+// non-negative itself and finite: its weights lie in [0, 1].  Every kernel
+// that writes sdf keeps the per-block count of such voxels (nnc) exact; the
+// raycast skips the gathers of samples whose corner blocks all count 512.
+__device__ __forceinline__ int sdf_nonneg(float s) { return s >= 0.0f && s < 1e30f ? 1 : 0; }
+// add the lanes' changes of one block's non-negative count (all active lanes
+// of the warp update the same block)
+__device__ __forceinline__ void note_nnc(const Dev &d, int blk, int delta) {
   const unsigned act = __activemask();
   const int sum = __reduce_add_sync(act, delta);
-  if ((int)lane_id() == __ffs(act) - 1 && sum) atomicAdd(d.posc + blk, sum);
+  if ((int)lane_id() == __ffs(act) - 1 && sum) atomicAdd(d.nnc + blk, sum);
 }
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;

@@ -19,8 +19,8 @@
 //    when a sample first needs an entry, so a sample's eight corners come
 //    from one branch-uniform gather;
 //  * exact skips (see ray_march): samples whose corner blocks hold only
-//    positive voxels are never gathered, and the t intervals inside missing
-//    blocks and inside all-positive blocks only advance t;
+//    non-negative voxels are never gathered, and the t intervals inside
+//    missing blocks and inside non-negative blocks only advance t;
 //  * 16x8-pixel CTAs keep neighbouring rays in one warp; they walk the same
 //    blocks at about the same t.
 #include "mh_internal.cuh"
@@ -52,18 +52,22 @@ struct RayCache {
 // the march itself, the lazily evaluated previous sample, the three
 // regula-falsi steps, the six gradient samples of the normal.  The first
 // corner's 2x2x2 block neighbourhood is a register table with three masks
-// (looked up, missing, all voxels positive), filled by hash lookups only when
-// a sample first needs an entry.
+// (looked up, missing, all voxels non-negative), filled by hash lookups only
+// when a sample first needs an entry.
 //
-// Skips, all exact.  A march sample is only needed for its sign, unless it is
-// negative right after a positive one; a sample whose corner blocks hold
-// only positive voxels (per-block count posc == 512) is positive and valid,
-// so its gather is skipped and it becomes the "previous sample" lazily: its
-// value is computed only when the next evaluated sample is negative.  Two
-// kinds of t interval are skipped with nothing but t += step: where the
-// first corner's block is missing (every sample invalid), and the interior
-// of an all-positive block where all eight corners lie in that block (every
-// sample valid and positive).
+// Skips, all exact.  A march sample matters only when it is negative right
+// after a positive one (the zero crossing), and then the previous sample's
+// value matters too.  A sample whose corner blocks hold only non-negative
+// voxels (per-block count nnc == 512) is valid and >= 0, so it can never be
+// the negative end of a crossing: its gather is skipped and it becomes the
+// "previous sample" lazily -- its value is computed only when the next
+// evaluated sample is negative, and the crossing is taken if that value is
+// > 0.  Three kinds of t interval are skipped with nothing but t += step:
+// where the first corner's block is missing (every sample invalid); where it
+// lies in a block flagged before the raycast (cellok: the block and its seven
+// upper neighbours exist and count 512, so every sample whose first corner
+// is there is valid and >= 0); and, otherwise, the interior of a block that
+// counts 512, where all eight corners lie in that block.
 namespace {
 
 enum { SM_OK = 0, SM_POS = 1, SM_MISS0 = 2, SM_MISS0_NEW = 3, SM_MISS = 4 };
@@ -72,7 +76,7 @@ struct Nbhd {
   int bx, by, bz;    // block of the first corner of the last sample
   unsigned looked;   // bit n: block n = (bx, by, bz) + (n & 1, n >> 1 & 1, n >> 2 & 1) looked up
   unsigned miss;     // bit n: block n is missing
-  unsigned pos;      // bit n: every voxel of block n is positive
+  unsigned pos;      // bit n: every voxel of block n is non-negative
   int p[8];          // block indices, indexed with constants only (registers)
   __device__ __forceinline__ void init() {
     bx = by = bz = 0x7fffffff;
@@ -84,7 +88,7 @@ struct Nbhd {
 
 // GetSpatialValue (geometry/spatial_query.h:23-66) with the same corners,
 // weights and summation order as spatial_sample.  Returns SM_OK with the
-// value in s, SM_POS when allow_pos and every corner block is all-positive
+// value in s, SM_POS when allow_pos and every corner block is non-negative
 // (value not computed), or why the sample is invalid.  b0_fresh: the first
 // corner's block was looked up by this call.
 __device__ __forceinline__ int nb_sample(const Dev &d, Nbhd &c, F3 pos, bool allow_pos, float &s, bool &b0_fresh) {
@@ -115,7 +119,7 @@ __device__ __forceinline__ int nb_sample(const Dev &d, Nbhd &c, F3 pos, bool all
     c.p[0] = q;
     if (q >= 0 && d.touch) d.touch[q] = 1;
     if (q < 0) c.miss |= 1u;
-    else if (__ldg(d.posc + q) == MH_BLOCK_VOXELS) c.pos |= 1u;
+    else if (__ldg(d.nnc + q) == MH_BLOCK_VOXELS) c.pos |= 1u;
     c.looked |= 1u;
     fresh &= ~1u;
   }
@@ -129,7 +133,7 @@ __device__ __forceinline__ int nb_sample(const Dev &d, Nbhd &c, F3 pos, bool all
       if (j == n) c.p[j] = q;
     if (q >= 0 && d.touch) d.touch[q] = 1;
     if (q < 0) c.miss |= 1u << n;
-    else if (__ldg(d.posc + q) == MH_BLOCK_VOXELS) c.pos |= 1u << n;
+    else if (__ldg(d.nnc + q) == MH_BLOCK_VOXELS) c.pos |= 1u << n;
   }
   c.looked |= need;
   if (need & c.miss) return SM_MISS;
@@ -273,6 +277,9 @@ __device__ __forceinline__ March ray_march(const Dev &d, F3 cam, F3 wd, float t_
         if (res == SM_MISS0_NEW) {
           block_interval(p, c.bx, c.by, c.bz, MH_BLOCK_SIDE, cam, wd, iwd, skip_lo, skip_hi);
           skip_pos = false;
+        } else if (res != SM_MISS0 && d.cellok && __ldg(d.cellok + c.p[0])) {
+          block_interval(p, c.bx, c.by, c.bz, MH_BLOCK_SIDE, cam, wd, iwd, skip_lo, skip_hi);
+          skip_pos = true;
         } else if (c.pos & 1u) {
           block_interval(p, c.bx, c.by, c.bz, MH_BLOCK_SIDE - 1, cam, wd, iwd, skip_lo, skip_hi);
           skip_pos = true;
@@ -299,9 +306,12 @@ __device__ __forceinline__ March ray_march(const Dev &d, F3 cam, F3 wd, float t_
     }
     if (phase == PH_PREV) {
       prev_lazy = false;
+      // the previous sample was valid; an invalid one here cannot happen
+      // while every sdf writer keeps nnc exact
+      if (res != SM_OK) set_error(d, MH_ERR_STATE);
       if (res != SM_OK || !(s > 0.0f)) {
-        // cannot happen while every sdf writer keeps posc exact
-        set_error(d, MH_ERR_STATE);
+        // no crossing (ray_caster.cu:87-88 needs prev > 0): the march goes on
+        // from the negative sample
         prev_sdf = cur_s, prev_t = t, have_prev = true;
         t += step;
         phase = PH_MARCH;
@@ -426,6 +436,33 @@ int launch_raycast_batch(const Scene *t, int n, int total, int shape, cudaStream
   return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
 }
 
+// Before a raycast: flag the candidate blocks whose own voxels and those of
+// their seven upper neighbours (the blocks at +1 in x, y, z and their
+// combinations, which a sample whose first corner lies in the block may
+// reach) all exist and count 512 non-negative voxels.  Blocks outside the
+// candidate list stay unflagged, which only turns their skip off.
+__global__ void __launch_bounds__(256) k_ray_cells(Dev d) {
+  const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int4 cb = d.cand[i];
+    if (cb.w < 0) continue;
+    bool ok = __ldg(d.nnc + cb.w) == MH_BLOCK_VOXELS;
+#pragma unroll 1
+    for (int j = 1; j < 8 && ok; ++j) {
+      const int q = hash_find(d, cb.x + (j & 1), cb.y + ((j >> 1) & 1), cb.z + ((j >> 2) & 1));
+      ok = q >= 0 && __ldg(d.nnc + q) == MH_BLOCK_VOXELS;
+    }
+    d.cellok[cb.w] = ok ? 1 : 0;
+  }
+}
+static int prepare_cells(const Dev &d, cudaStream_t s) {
+  if (!d.cellok) return MH_OK;
+  MH_CUDA_TRY(cudaMemsetAsync(d.cellok, 0, (size_t)d.p.value_capacity, s));
+  k_ray_cells<<<mh_sm_count() * 8, 256, 0, s>>>(d);
+  mh_count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? MH_OK : MH_ERR_CUDA;
+}
+
 // number of nonzero bytes of flags[0, n) added to *out
 __global__ void k_count_flags(const uint8_t *flags, int n, int *out) {
   int c = 0;
@@ -440,6 +477,8 @@ int launch_count_flags(const uint8_t *flags, int n, int *out, cudaStream_t s) {
 }
 
 int launch_raycast(const Dev &d, float *depth, float *vert4, float *norm4, cudaStream_t s) {
+  const int r = prepare_cells(d, s);
+  if (r != MH_OK) return r;
   dim3 blk(RC_TX, RC_TY);
   dim3 grid((d.p.rc_width + RC_TX - 1) / RC_TX, (d.p.rc_height + RC_TY - 1) / RC_TY);
   k_raycast<<<grid, blk, 0, s>>>(d, depth, reinterpret_cast<float4 *>(vert4), reinterpret_cast<float4 *>(norm4));
@@ -767,6 +806,8 @@ __global__ void __launch_bounds__(RC_TX *RC_TY) k_raycast_grad(Dev d, int mode, 
 
 int launch_raycast_grad(const Dev &d, int mode, const float *dLdD, const float *dLdN4, float *grad, const float *obs,
                         float max_res, double *acc, cudaStream_t s) {
+  const int r = prepare_cells(d, s);
+  if (r != MH_OK) return r;
   dim3 blk(RC_TX, RC_TY);
   dim3 grid((d.p.rc_width + RC_TX - 1) / RC_TX, (d.p.rc_height + RC_TY - 1) / RC_TY);
   k_raycast_grad<<<grid, blk, 0, s>>>(d, mode, dLdD, reinterpret_cast<const float4 *>(dLdN4), grad, obs, max_res,

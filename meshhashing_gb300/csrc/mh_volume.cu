@@ -137,7 +137,7 @@ __global__ void k_scatter_fields(Dev d, const int *ptr, int n, const float *sdf,
     if (v == 0) d.wmax[p] = __int_as_float(0x7f800000);
     if (sdf) {
       d.sdf[dst] = sdf[src];
-      mine += sdf_positive(sdf[src]);
+      mine += sdf_nonneg(sdf[src]);
     }
     if (w) d.w[dst] = w[src];
     if (a) d.a[dst] = a[src];
@@ -146,7 +146,7 @@ __global__ void k_scatter_fields(Dev d, const int *ptr, int n, const float *sdf,
   if (sdf) {
     atomicAdd(&npos, mine);
     __syncthreads();
-    if (threadIdx.x == 0) d.posc[p] = npos;
+    if (threadIdx.x == 0) d.nnc[p] = npos;
   }
 }
 
@@ -244,7 +244,7 @@ int mh_volume_reset(mh_volume *v, void *stream) {
   MH_CUDA_TRY(cudaMemsetAsync(d.boundary, 0, sizeof(int) * cap, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.nvtx, 0, sizeof(int) * cap, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.wmax, 0, sizeof(float) * cap, s));
-  MH_CUDA_TRY(cudaMemsetAsync(d.posc, 0, sizeof(int) * cap, s));
+  MH_CUDA_TRY(cudaMemsetAsync(d.nnc, 0, sizeof(int) * cap, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.page_of, 0xFF, sizeof(int) * cap, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.page_owner, 0xFF, sizeof(int) * (size_t)npg, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.cube, 0, pv, s));
@@ -351,7 +351,8 @@ int mh_volume_create(const mh_params *p, mh_volume **out) {
   const size_t pv = (size_t)d.page_capacity * MH_BLOCK_VOXELS;
   A(dalloc(v, &d.page_of, cap));
   A(dalloc(v, &d.wmax, cap));
-  A(dalloc(v, &d.posc, cap));
+  A(dalloc(v, &d.nnc, cap));
+  A(dalloc(v, &d.cellok, cap));
   A(dalloc(v, &d.mesh_list, cap));
   A(dalloc(v, &d.cube_list, cap));
   A(dalloc(v, &d.vtx_list, cap));
@@ -877,14 +878,14 @@ int mh_dump_block_meta(mh_volume *v, int n, const int32_t *pos, int32_t *life, i
   return MH_OK;
 }
 
-int mh_dump_positive_counts(mh_volume *v, int n, const int32_t *pos, int32_t *count) {
+int mh_dump_nonneg_counts(mh_volume *v, int n, const int32_t *pos, int32_t *count) {
   CHECK_VOL(v);
   if (n < 0 || (n > 0 && (!pos || !count))) return MH_ERR_INVALID;
   MH_CUDA_TRY(cudaDeviceSynchronize());
   std::vector<int> ptr;
   TRY(find_ptrs(v, n, pos, ptr, false));
   std::vector<int> all((size_t)v->d.p.value_capacity);
-  MH_CUDA_TRY(cudaMemcpy(all.data(), v->d.posc, sizeof(int) * all.size(), cudaMemcpyDeviceToHost));
+  MH_CUDA_TRY(cudaMemcpy(all.data(), v->d.nnc, sizeof(int) * all.size(), cudaMemcpyDeviceToHost));
   for (int i = 0; i < n; ++i) count[i] = ptr[i] < 0 ? INT32_MIN : all[ptr[i]];
   return MH_OK;
 }

@@ -370,11 +370,11 @@ class Volume:
                 _ptr(bnd, C.c_int32))
         return life, inner, bnd
 
-    def positive_counts(self, pos):
-        """Per block: the library's count of voxels with sdf in (1e-30, 1e30)."""
+    def nonneg_counts(self, pos):
+        """Per block: the library's count of voxels with sdf in [0, 1e30)."""
         pos = _i32(pos).reshape(-1, 3)
         out = np.zeros(len(pos), np.int32)
-        self._c("mh_dump_positive_counts", len(pos), _ptr(pos, C.c_int32), _ptr(out, C.c_int32))
+        self._c("mh_dump_nonneg_counts", len(pos), _ptr(pos, C.c_int32), _ptr(out, C.c_int32))
         return out
 
     def flags(self):

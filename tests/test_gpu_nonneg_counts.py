@@ -1,9 +1,9 @@
-"""The per-block positive-voxel counts the raycast's skips rely on.
+"""The per-block non-negative-voxel counts the raycast's skips rely on.
 
 Every kernel that writes sdf keeps, per block, the number of voxels whose
-sdf lies in (1e-30, 1e30) (mh_dump_positive_counts); the raycast skips the
-gathers of samples whose corner blocks all count 512, and the interiors of
-such blocks.  A stale count would change the raycast's output, so the counts
+sdf lies in [0, 1e30) (mh_dump_nonneg_counts); the raycast skips the gathers
+of samples whose corner blocks all count 512, the interiors of such blocks,
+and whole blocks whose seven upper neighbours count 512 too.  A stale count would change the raycast's output, so the counts
 are checked against a recount from the voxels after every kind of writer:
 the simple and the PSDF update, the GC that frees blocks (recycle every 10
 frames, starvation in simple mode), the volumetric Huber-TV, and
@@ -20,12 +20,12 @@ pytestmark = pytest.mark.gpu
 
 
 def recount(sdf):
-    return ((sdf > np.float32(1e-30)) & (sdf < np.float32(1e30))).sum(axis=1).astype(np.int32)
+    return ((sdf >= np.float32(0.0)) & (sdf < np.float32(1e30))).sum(axis=1).astype(np.int32)
 
 
 def check_counts(v, what):
     pos, f = v.dump_blocks(("sdf",))
-    got = v.positive_counts(pos)
+    got = v.nonneg_counts(pos)
     want = recount(f["sdf"])
     bad = np.nonzero(got != want)[0]
     assert bad.size == 0, f"{what}: {bad.size} of {len(pos)} blocks have stale counts"
