@@ -182,7 +182,7 @@ __device__ __forceinline__ void gc_recycle_vtx_body(const Dev &d) {
       d.boundary[ptr] = 0;
       d.nvtx[ptr] = 0;
       d.wmax[ptr] = 0.0f;
-      d.nnc[ptr] = 0;  // its voxels are zeroed below
+      d.nnc[ptr] = MH_BLOCK_VOXELS;  // its voxels are zeroed below (sdf 0 is non-negative)
       d.cand[c].w = -1;
       atomicAdd(&d.ctr->gc_freed, 1);
     }

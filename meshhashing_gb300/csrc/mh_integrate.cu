@@ -18,12 +18,15 @@ namespace {
 struct VoxProj {
   float cam_z;
   float depth;
+  float aux;
   int pix;
 };
 
-// Per-voxel projection shared by the update kernels (update_simple.cu:26-46)
-__device__ __forceinline__ bool project_voxel(const DevParams &p, const float *cTw, const float *depth, int vx,
-                                              int vy, int vz, VoxProj &o) {
+// Per-voxel projection shared by the update kernels (update_simple.cu:26-46).
+// `aux` (the inlier ratio of the PSDF update, or null) is read at the same
+// pixel in the same round trip as the depth.
+__device__ __forceinline__ bool project_voxel(const DevParams &p, const float *cTw, const float *depth,
+                                              const float *aux, int vx, int vy, int vz, VoxProj &o) {
   const float vs = p.voxel_size;
   F3 c = mul_pt(cTw, f3((float)vx * vs, (float)vy * vs, (float)vz * vs));
   const float u = c.x * p.fx / c.z + p.cx;
@@ -32,6 +35,7 @@ __device__ __forceinline__ bool project_voxel(const DevParams &p, const float *c
   if (px >= p.width || py >= p.height) return false;
   const int pix = py * p.width + px;
   const float d = __ldg(depth + pix);
+  o.aux = aux ? __ldg(aux + pix) : 0.0f;
   if (depth_invalid(p, d)) return false;
   o.cam_z = c.z;
   o.depth = d;
@@ -66,8 +70,11 @@ __device__ __forceinline__ void integrate_simple_body(const Dev &d) {
   const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
   const int t = threadIdx.x;
   const int lx = (t & 1) * 4, ly = (t >> 1) & 7, lz = t >> 4;
+  // the next candidate is fetched one iteration ahead
+  int4 next = (int)blockIdx.x < n ? d.cand[blockIdx.x] : make_int4(0, 0, 0, -1);
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
-    const int4 cb = d.cand[c];
+    const int4 cb = next;
+    if (c + (int)gridDim.x < n) next = d.cand[c + gridDim.x];
     if (cb.w < 0) continue;
     const int vx0 = cb.x * MH_BLOCK_SIDE + lx, vy = cb.y * MH_BLOCK_SIDE + ly, vz = cb.z * MH_BLOCK_SIDE + lz;
     float sdf_new[4], w_new[4];
@@ -76,7 +83,7 @@ __device__ __forceinline__ void integrate_simple_body(const Dev &d) {
     for (int k = 0; k < 4; ++k) {
       VoxProj o;
       act[k] = false;
-      if (!project_voxel(p, cTw, d.depth, vx0 + k, vy, vz, o)) continue;
+      if (!project_voxel(p, cTw, d.depth, nullptr, vx0 + k, vy, vz, o)) continue;
       float sdf = o.depth - o.cam_z;
       // 1 - normalized depth as (dmax - d) / (dmax - dmin): same value, no
       // cancellation near the far limit (update_simple.cu:49-55); the
@@ -119,7 +126,7 @@ __global__ void __launch_bounds__(128) k_integrate_simple_b(const Scene *t, int 
 
 // UpdateBlocksBayesianKernel (mapping/update_bayesian.cu:103-185).  Per voxel
 // the update is division- and transcendental-bound, not load-bound, so the
-// default form regroups it to 10 IEEE divisions (see below); compat mode
+// default form restates it with 4 IEEE divisions (see below); compat mode
 // evaluates the reference's expressions as written.
 __device__ __forceinline__ void integrate_psdf_body(const Dev &d) {
   __shared__ float cTw[16];
@@ -129,8 +136,10 @@ __device__ __forceinline__ void integrate_psdf_body(const Dev &d) {
   const int n = *reinterpret_cast<volatile int *>(&d.ctr->cand_count);
   const int t = threadIdx.x;
   const int lx = (t & 1) * 4, ly = (t >> 1) & 7, lz = t >> 4;
+  int4 next = (int)blockIdx.x < n ? d.cand[blockIdx.x] : make_int4(0, 0, 0, -1);
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
-    const int4 cb = d.cand[c];
+    const int4 cb = next;
+    if (c + (int)gridDim.x < n) next = d.cand[c + gridDim.x];
     if (cb.w < 0) continue;
     const int vx0 = cb.x * MH_BLOCK_SIDE + lx, vy = cb.y * MH_BLOCK_SIDE + ly, vz = cb.z * MH_BLOCK_SIDE + lz;
     float xs[4], rho[4], dep[4];
@@ -139,9 +148,9 @@ __device__ __forceinline__ void integrate_psdf_body(const Dev &d) {
     for (int k = 0; k < 4; ++k) {
       VoxProj o;
       act[k] = false;
-      if (!project_voxel(p, cTw, d.depth, vx0 + k, vy, vz, o)) continue;
+      if (!project_voxel(p, cTw, d.depth, d.inlier, vx0 + k, vy, vz, o)) continue;
       float x = o.depth - o.cam_z;
-      const float r = __ldg(d.inlier + o.pix);
+      const float r = o.aux;
       const float tr = truncate_dist(p, o.depth);
       if (x <= -tr) continue;
       x = x >= 0.0f ? fminf(tr, x) : fmaxf(-tr, x);
@@ -201,38 +210,36 @@ __device__ __forceinline__ void integrate_psdf_body(const Dev &d) {
         put(B, k, na * (1.0f - f) / f);
         continue;
       }
-      // The same update with 10 divisions instead of 21: 1/s2 is the stored
-      // weight itself, reciprocals are shared, f and e are put over common
-      // denominators, (e - f) / (f - e/f) is taken as f (e - f) / (f^2 - e),
-      // and the variance is C1 s^2 + C2 sigma^2 + C1 C2 (m - mu)^2, equal to
-      // the reference's C1 (s^2 + m^2) + C2 (sigma^2 + mu^2) - sdf'^2 when
-      // C1 + C2 = 1 but free of its cancellation.
-      const float s2 = 1.0f / w0;
-      const float it2 = 1.0f / t2;
-      const float ss2 = 1.0f / (w0 + it2);
-      const float m = ss2 * (mu * w0 + x * it2);
-      const float sv = s2 + t2;
-      const float isv = 1.0f / sv;
+      // The same update with 4 divisions instead of 21.  With the stored
+      // weight w0 = 1/s^2 and u = w0 sigma^2, q = 1/(1 + u):
+      //   the product's variance s~^2 = sigma^2 q, its mean m = q (mu u + x),
+      //   1/(s^2 + sigma^2) = w0 q, so gaussian() = exp(-dx^2 w0 q) sqrt(w0 q) / sqrt(2 pi);
+      //   c = C1 / (C1 + C2) is the normalised inlier weight, 1 - c the outlier's;
+      //   sdf' = mu + c (m - mu);
+      //   the variance c s~^2 + (1 - c) s^2 + c (1 - c)(m - mu)^2 (the
+      //   reference's C1 (s~^2 + m^2) + C2 (s^2 + mu^2) - sdf'^2 without its
+      //   cancellation) gives w' = w0 / (c u q + (1 - c) + c (1 - c)(m - mu)^2 w0);
+      //   the Beta moments f, e of the reference give a' = f (e - f) / (f^2 - e)
+      //   = (a + c) k and b' = a' (1 - f) / f = (b + 1 - c) k with
+      //   k = (c (a - b) - a (b + 1)) / (c^2 (a + b + 2) - (a + 2c)(b + 1)),
+      //   which cancels far less than f^2 - e.
+      const float u = w0 * t2;
+      const float q = 1.0f / (1.0f + u);
+      const float m = q * (mu * u + x);
+      const float isv = w0 * q;
       const float dx = x - mu;
-      // gaussian(): exp(-dx^2 / sv) / sqrt(2 pi sv)
-      const float g = mh_expf(-(dx * dx) * isv) * (sqrtf(sv) * isv) * 0.398942280401432678f;
-      float C1 = r * g;
-      float C2 = in_range ? (1.0f - r) * 0.204081632653061224f : 1.0f;
-      const float isum = 1.0f / (C1 + C2);
-      C1 *= isum;
-      C2 *= isum;
-      const float ab1 = a + b + 1.0f;
-      const float iab1 = 1.0f / ab1;
-      const float f = (C1 * (a + 1.0f) + C2 * a) * iab1;
-      const float e = (a + 1.0f) * (C1 * (a + 2.0f) + C2 * a) * iab1 / (ab1 + 1.0f);
-      const float nsdf = C1 * m + C2 * mu;
+      const float g = mh_expf(-(dx * dx) * isv) * sqrtf(isv) * 0.398942280401432678f;
+      const float C1 = r * g;
+      const float C2 = in_range ? (1.0f - r) * 0.204081632653061224f : 1.0f;
+      const float c = C1 / (C1 + C2);
+      const float oc = 1.0f - c;
       const float dm = m - mu;
-      const float var = C1 * ss2 + C2 * s2 + C1 * C2 * (dm * dm);
-      put(S, k, nsdf);
-      put(W, k, 1.0f / var);
-      const float na = f * (e - f) / (f * f - e);
-      put(A, k, na);
-      put(B, k, na * (1.0f - f) / f);
+      put(S, k, mu + c * dm);
+      put(W, k, w0 / (c * u * q + oc + c * oc * (dm * dm) * w0));
+      const float b1 = b + 1.0f;
+      const float kk = (c * (a - b) - a * b1) / (c * c * (a + b + 2.0f) - (a + 2.0f * c) * b1);
+      put(A, k, (a + c) * kk);
+      put(B, k, (b1 - c) * kk);
     }
     *reinterpret_cast<float4 *>(d.sdf + base) = S;
     *reinterpret_cast<float4 *>(d.w + base) = W;
@@ -242,7 +249,7 @@ __device__ __forceinline__ void integrate_psdf_body(const Dev &d) {
     note_nnc(d, cb.w, sdf_nonneg(S.x) + sdf_nonneg(S.y) + sdf_nonneg(S.z) + sdf_nonneg(S.w) - pos_before);
   }
 }
-__global__ void __launch_bounds__(128) k_integrate_psdf(Dev d) { integrate_psdf_body(d); }
+__global__ void __launch_bounds__(128, 8) k_integrate_psdf(Dev d) { integrate_psdf_body(d); }
 __global__ void __launch_bounds__(128) k_integrate_psdf_b(const Scene *t, int n) {
   each_scene(t, n, [&](const Scene &c) { if (c.d.p.enable_bayesian) integrate_psdf_body(c.d); });
 }
@@ -277,7 +284,7 @@ __device__ __forceinline__ void predict_inlier_body(const Dev &d) {
     for (int k = 0; k < 4; ++k) {
       if (slots[3 * k] <= 0 && slots[3 * k + 1] <= 0 && slots[3 * k + 2] <= 0) continue;
       VoxProj o;
-      if (!project_voxel(p, cTw, d.depth, vx0 + k, vy, vz, o)) continue;
+      if (!project_voxel(p, cTw, d.depth, nullptr, vx0 + k, vy, vz, o)) continue;
       const int px = o.pix % p.width, py = o.pix / p.width;
       const float rx = ((float)px - p.cx) / p.fx, ry = ((float)py - p.cy) / p.fy;
       const F3 pc = f3(o.depth * rx, o.depth * ry, o.depth);

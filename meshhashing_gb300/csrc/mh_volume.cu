@@ -244,7 +244,6 @@ int mh_volume_reset(mh_volume *v, void *stream) {
   MH_CUDA_TRY(cudaMemsetAsync(d.boundary, 0, sizeof(int) * cap, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.nvtx, 0, sizeof(int) * cap, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.wmax, 0, sizeof(float) * cap, s));
-  MH_CUDA_TRY(cudaMemsetAsync(d.nnc, 0, sizeof(int) * cap, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.page_of, 0xFF, sizeof(int) * cap, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.page_owner, 0xFF, sizeof(int) * (size_t)npg, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.cube, 0, pv, s));
@@ -252,6 +251,8 @@ int mh_volume_reset(mh_volume *v, void *stream) {
   MH_CUDA_TRY(cudaMemsetAsync(d.vtx, 0, sizeof(Vertex) * (size_t)P.max_vertex_count, s));
   MH_CUDA_TRY(cudaMemsetAsync(d.flags, 0, cap, s));
   k_fill_i32<<<grid_for(cap), 256, 0, s>>>(d.life, cap, MH_BLOCK_LIFE);
+  // every voxel starts at sdf 0, which counts as non-negative
+  k_fill_i32<<<grid_for(cap), 256, 0, s>>>(d.nnc, cap, MH_BLOCK_VOXELS);
   k_fill_i32<<<grid_for(pv * 3), 256, 0, s>>>(d.vtx_slot, pv * 3, MH_FREE_PTR);
   k_fill_i32<<<grid_for(pv * 5), 256, 0, s>>>(d.tri_slot, pv * 5, MH_FREE_PTR);
   k_stack_init<<<grid_for(npg), 256, 0, s>>>(d.page_heap, (int)npg, (int)npg);

@@ -704,37 +704,33 @@ template <class R> struct Vol {
         R t2 = tau * tau;
         const bool in_range = d < (R)p.max_depth_range && d >= (R)p.min_depth_range;
         if (sizeof(R) == 4 && !p.compat_arithmetic) {
-          // the single-precision form of the library: 10 divisions, same
-          // operation order (1/s2 is the stored weight, shared reciprocals,
-          // f and e over common denominators, f (e - f) / (f^2 - e), and the
-          // variance as C1 s^2 + C2 sigma^2 + C1 C2 (m - mu)^2)
+          // the single-precision form of the library, same operation order:
+          // 4 divisions, with u = w0 sigma^2 and q = 1 / (1 + u) the product's
+          // variance is sigma^2 q and its mean q (mu u + x); c = C1 / (C1 + C2);
+          // sdf' = mu + c (m - mu); w' = w0 / (c u q + (1 - c) + c (1 - c)(m - mu)^2 w0);
+          // a' = (a + c) k, b' = (b + 1 - c) k with
+          // k = (c (a - b) - a (b + 1)) / (c^2 (a + b + 2) - (a + 2c)(b + 1)),
+          // the reference's Beta moments f (e - f) / (f^2 - e) and a' (1 - f) / f
+          // put over one denominator
           const float w0 = (float)b->w[i], muf = (float)mu, xf = (float)x, rf = (float)rho, t2f = (float)t2;
           const float af = (float)a, bf = (float)bb;
-          const float s2 = 1.0f / w0;
-          const float it2 = 1.0f / t2f;
-          const float ss2 = 1.0f / (w0 + it2);
-          const float m = ss2 * (muf * w0 + xf * it2);
-          const float sv = s2 + t2f;
-          const float isv = 1.0f / sv;
+          const float u = w0 * t2f;
+          const float q = 1.0f / (1.0f + u);
+          const float m = q * (muf * u + xf);
+          const float isv = w0 * q;
           const float dx = xf - muf;
-          const float g = mh_expf(-(dx * dx) * isv) * (std::sqrt(sv) * isv) * 0.398942280401432678f;
-          float C1 = rf * g;
-          float C2 = in_range ? (1.0f - rf) * 0.204081632653061224f : 1.0f;
-          const float isum = 1.0f / (C1 + C2);
-          C1 *= isum;
-          C2 *= isum;
-          const float ab1 = af + bf + 1.0f;
-          const float iab1 = 1.0f / ab1;
-          const float f = (C1 * (af + 1.0f) + C2 * af) * iab1;
-          const float e = (af + 1.0f) * (C1 * (af + 2.0f) + C2 * af) * iab1 / (ab1 + 1.0f);
-          const float nsdf = C1 * m + C2 * muf;
+          const float g = mh_expf(-(dx * dx) * isv) * std::sqrt(isv) * 0.398942280401432678f;
+          const float C1 = rf * g;
+          const float C2 = in_range ? (1.0f - rf) * 0.204081632653061224f : 1.0f;
+          const float c = C1 / (C1 + C2);
+          const float oc = 1.0f - c;
           const float dm = m - muf;
-          const float var = C1 * ss2 + C2 * s2 + C1 * C2 * (dm * dm);
-          const float na = f * (e - f) / (f * f - e);
-          b->sdf[i] = nsdf;
-          b->w[i] = 1.0f / var;
-          b->a[i] = na;
-          b->b[i] = na * (1.0f - f) / f;
+          b->sdf[i] = muf + c * dm;
+          b->w[i] = w0 / (c * u * q + oc + c * oc * (dm * dm) * w0);
+          const float b1 = bf + 1.0f;
+          const float kk = (c * (af - bf) - af * b1) / (c * c * (af + bf + 2.0f) - (af + 2.0f * c) * b1);
+          b->a[i] = (af + c) * kk;
+          b->b[i] = (b1 - c) * kk;
           continue;
         }
         // the reference's expressions (update_bayesian.cu:140-180): in double

@@ -140,9 +140,10 @@ def test_oracle_fp32_close_to_fp64(built):
 
 def test_oracle_psdf_fp32_close_to_fp64(built):
     """One PSDF update from the same state and inlier image in each precision:
-    the single-precision form (10 divisions, regrouped) against the
-    reference's expressions evaluated in double.  Weights and the inlier
-    Beta parameters within 1e-5 relative; sdf within 2e-6 m absolute, the
+    the single-precision form (4 divisions, restated) against the
+    reference's expressions evaluated in double.  Weights within 1e-5 and
+    the inlier Beta parameters within 5e-6 relative (1.4e-6 measured: the
+    restated a', b' avoid the cancellation of f^2 - e); sdf within 2e-6 m absolute, the
     rounding of a single-precision camera depth of a few metres, which both
     forms share (a relative bound is meaningless at the zero crossing)."""
     wl = scene.full_spline(40, width=160, height=120)
@@ -181,8 +182,8 @@ def test_oracle_psdf_fp32_close_to_fp64(built):
     assert later.sum() > 100000
     assert np.abs(g - o)[upd].max() < 2e-6
     assert (np.abs(gw - ow)[upd] / ow[upd]).max() < 1e-5
-    assert (np.abs(ga - oa)[later] / np.abs(oa[later])).max() < 1e-5
-    assert (np.abs(gb - ob)[later] / np.abs(ob[later])).max() < 1e-5
+    assert (np.abs(ga - oa)[later] / np.abs(oa[later])).max() < 5e-6
+    assert (np.abs(gb - ob)[later] / np.abs(ob[later])).max() < 5e-6
 
 
 def test_oracle_raycast_hits_the_scene(built):
