@@ -744,15 +744,20 @@ def main():
     per_launch_ms = stage_ms[dom] / calls
     alg = bytes_per_launch(dom, nb, px, rpx, vwork, **counts)
     achieved = alg / (per_launch_ms / 1000.0) / 1e9
-    # DRAM bytes per launch measured by ncu (dram__bytes_read.sum + _write.sum)
-    # on this workload at 454,148 candidate blocks, scaled by this run's count
-    NCU_TRAFFIC = {"raycast": (392.1e6, 454148.0), "integrate": (3.04e9, 454148.0)}
+    # DRAM bytes per launch measured by ncu (dram__bytes_read.sum + _write.sum,
+    # --set full) on this workload's 10-frame map (frame 9: 274,742 candidate
+    # blocks, 143,854 of them looked up by rays), scaled to this run by the
+    # units the kernel's traffic follows: blocks the rays look up for the
+    # raycast, candidate blocks for the integrate
+    NCU_TRAFFIC = {"raycast": (116.87e6, 143854.0, "ray_blocks", "blocks looked up by rays"),
+                   "integrate": (1780.52e6, 274742.0, "candidates", "candidate blocks")}
     traffic, traffic_src = None, None
     if dom in NCU_TRAFFIC:
-        b0, n0 = NCU_TRAFFIC[dom]
-        traffic = b0 * nb / n0
-        traffic_src = ("ncu DRAM read+write of one launch at %d candidate blocks (frames 44-45 of this workload), "
-                       "scaled by candidate blocks" % int(n0))
+        b0, n0, unit, what = NCU_TRAFFIC[dom]
+        n1 = ray_blocks if unit == "ray_blocks" else nb
+        traffic = b0 * n1 / n0
+        traffic_src = ("ncu DRAM read+write of one launch at %d %s (frame 9 of this workload, 10-frame map), "
+                       "scaled by %s" % (int(n0), what, what))
     stages = {}
     for k, (t_ms, c) in prof.items():
         if c:
