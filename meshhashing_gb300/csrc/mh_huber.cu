@@ -128,7 +128,6 @@ __global__ void __launch_bounds__(256) k_pd_list(Dev d, PD pd, unsigned *list, i
   for (int c = blockIdx.x; c < n; c += gridDim.x) {
     const int blk = d.cand[c].w;
     bool f[2];
-    int mine = 0;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const long long g = (long long)blk * MH_BLOCK_VOXELS + threadIdx.x + 256 * h;

@@ -406,7 +406,9 @@ __device__ __forceinline__ void raycast_body(const Dev &d, int tile_x, int tile_
   if (out_vert) out_vert[pix] = o_vert;
   if (out_norm) out_norm[pix] = o_norm;
 }
-__global__ void __launch_bounds__(RC_TX *RC_TY) k_raycast(Dev d, float *out_depth, float4 *out_vert, float4 *out_norm) { raycast_body<RC_TX, RC_TY>(d, blockIdx.x, blockIdx.y, out_depth, out_vert, out_norm); }
+// six resident CTAs per SM (at most 80 registers; a few bytes spill) ran
+// 1.5 % faster than the five that 86 registers allow, with the same output
+__global__ void __launch_bounds__(RC_TX *RC_TY, 6) k_raycast(Dev d, float *out_depth, float4 *out_vert, float4 *out_norm) { raycast_body<RC_TX, RC_TY>(d, blockIdx.x, blockIdx.y, out_depth, out_vert, out_norm); }
 // batched raycast over the scenes' concatenated TX x TY tiles; the tile shape
 // is an autotuned choice (the scene table's ray_tile0 follows it)
 template <int TX, int TY>
