@@ -21,6 +21,10 @@ def _torch():
     return torch
 
 
+def _device(volume):
+    return getattr(volume, "torch_device", "cuda")
+
+
 class SdfVoxels:
     """Voxels of a Volume whose sdf values form one torch input.
 
@@ -48,12 +52,13 @@ class SdfVoxels:
         self.rows = np.stack([f["sdf"][lut[tuple(b)]] for b in self.blocks.tolist()]).astype(np.float32)
         # pool index of each block: a field whose first voxel of pool entry i holds i
         cap = volume.params.value_capacity
-        probe = torch.zeros((cap, 512), dtype=torch.float32, device="cuda")
-        probe[:, 0] = torch.arange(cap, dtype=torch.float32, device="cuda")
+        dev = _device(volume)
+        probe = torch.zeros((cap, 512), dtype=torch.float32, device=dev)
+        probe[:, 0] = torch.arange(cap, dtype=torch.float32, device=dev)
         ppos, prows = volume.dump_block_field(probe)
         pool = {tuple(q): int(r[0]) for q, r in zip(ppos.tolist(), prows)}
         block_pool = np.array([pool[tuple(b)] for b in self.blocks.tolist()], np.int64)
-        self.flat = torch.from_numpy(block_pool[self.row_of] * 512 + self.vidx).cuda()
+        self.flat = torch.from_numpy(block_pool[self.row_of] * 512 + self.vidx).to(dev)
 
     def values(self) -> np.ndarray:
         """The voxels' current sdf values (float32)."""
@@ -72,9 +77,9 @@ def _render(volume, xi, wTc0):
     torch = _torch()
     T = left_update(np.asarray(wTc0, np.float64), xi.detach().cpu().numpy().astype(np.float64))
     cTw = np.linalg.inv(T).astype(np.float32)
-    H, W = volume.RH, volume.RW
-    depth = torch.empty((H, W), dtype=torch.float32, device="cuda")
-    normal = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+    H, W, dev = volume.RH, volume.RW, _device(volume)
+    depth = torch.empty((H, W), dtype=torch.float32, device=dev)
+    normal = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
     volume.raycast(cTw, depth_out=depth, normal_out=normal)
     hit = torch.isfinite(depth)
     return cTw, torch.where(hit, depth, torch.zeros_like(depth)), torch.where(
@@ -83,12 +88,12 @@ def _render(volume, xi, wTc0):
 
 def _backward(volume, cTw, g_depth, g_normal, grad_sdf=None):
     torch = _torch()
-    H, W = volume.RH, volume.RW
+    H, W, dev = volume.RH, volume.RW, _device(volume)
     gd = g_depth.contiguous().float() if g_depth is not None else torch.zeros((H, W), dtype=torch.float32,
-                                                                               device="cuda")
+                                                                               device=dev)
     gn = None
     if g_normal is not None:
-        gn = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+        gn = torch.zeros((H, W, 4), dtype=torch.float32, device=dev)
         gn[..., :3] = g_normal
     return volume.raycast_backward(cTw, gd, gn, grad_sdf)
 
@@ -145,7 +150,7 @@ def _functions():
         @staticmethod
         def backward(ctx, g_depth, g_normal):
             v = ctx.voxels.volume
-            g = torch.zeros(v.params.value_capacity * 512, dtype=torch.float32, device="cuda")
+            g = torch.zeros(v.params.value_capacity * 512, dtype=torch.float32, device=_device(v))
             dxi = _backward(v, ctx.cTw, g_depth, g_normal, g)
             gs = ctx.voxels.gather(g).to(dtype=ctx.sdf_dtype, device=ctx.sdf_device)
             return torch.tensor(dxi, dtype=ctx.xi_dtype, device=ctx.xi_device), gs, None, None

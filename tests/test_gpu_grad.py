@@ -183,101 +183,14 @@ def test_refine_pose_from_perturbed_start(built):
 def test_autograd_gradcheck_pose_and_voxel_sdf(built):
     """torch.autograd.gradcheck of rendered depth with respect to the pose
     increment and up to eight voxel sdf values together (RaycastPoseSdf),
-    against central differences (h = 1e-4) of the GPU's own forward.
-
-    * The sdf input enters as s0 + 0.3 z, so gradcheck's step moves a voxel
-      by 3e-5 m: the regula falsi divides sdf differences of a few
-      millimetres, and a 1e-4 m step would bend the difference quotient by
-      a few percent.
-    * Pixels closer than 3 m whose depth is smooth in the pose across the
-      stencil (second difference within 1 % of the first: a kink inside the
-      stencil, where the hit crosses a cell face, shows as a larger one) are
-      drawn at random; each contributes the voxel with the largest sdf
-      gradient of its depth among voxels with |sdf| >= 1e-4 m (no sign
-      change under the step).
-    * The outputs are up to 12 pixels that those voxels move and 12 that
-      they do not (zero sdf gradient), all smooth in every input (3 % for the
-      sdf steps, which bend the regula falsi more).  The tolerance covers a
-      few float32 ulps of those depths over the 2h stencil."""
-    torch = pytest.importorskip("torch")
-    from meshhashing_gb300.autograd import RaycastPoseSdf, SdfVoxels
-    SCALE = 0.3
+    against central differences (h = 1e-4) of the GPU's own forward; the
+    procedure is tests/_gradcheck.py's."""
+    pytest.importorskip("torch")
+    from tests._gradcheck import check_pose_sdf
     wl, p, v = _setup(width=128, height=96)
-    T0 = wl.pose(34).astype(np.float64)
-    cTw = np.linalg.inv(T0).astype(np.float32)
-    d0, _, _ = v.raycast(cTw)
-    bpos, bf = v.dump_blocks(fields=("sdf",))
-    rows = {tuple(q): r for q, r in zip(bpos.tolist(), bf["sdf"])}
 
-    def smooth(dp, dm, c, rel):
-        with np.errstate(invalid="ignore"):
-            return np.isfinite(dp) & np.isfinite(dm) & (np.abs(dp + dm - 2 * c) <= 3e-6 + rel * np.abs(dp - dm))
+    def block_grad(v, cTw, a):
+        _, gp, gr = _gpu_backward(v, cTw, a)
+        return gp, gr
 
-    def render(xi):
-        d, _, _ = v.raycast(np.linalg.inv(left_update(T0, xi)).astype(np.float32))
-        return d.astype(np.float64)
-
-    base = d0.astype(np.float64)
-    keep = np.isfinite(base) & (base < 3.0)
-    for k in range(6):
-        e = np.zeros(6)
-        e[k] = H_FD
-        keep &= smooth(render(e), render(-e), base, 0.01)
-    rng = np.random.default_rng(7)
-    vox = []
-    for px in rng.choice(np.flatnonzero(keep.reshape(-1)), 16, replace=False):
-        a = np.zeros(base.size)
-        a[px] = 1.0
-        _, gp, gr = _gpu_backward(v, cTw, a.reshape(base.shape))
-        sdf_of = np.stack([rows[tuple(q)] for q in gp.tolist()]).reshape(-1)
-        score = np.where(np.abs(sdf_of) >= 1e-4, np.abs(gr).reshape(-1), 0.0)
-        j = int(np.argmax(score))
-        cand = [*gp[j // 512], j % 512]
-        if score[j] > 0 and cand not in vox:
-            vox.append(cand)
-        if len(vox) == 8:
-            break
-    assert len(vox) >= 4
-    sv = SdfVoxels(v, np.array(vox))
-    s0 = sv.values().astype(np.float64)
-
-    def depth_at(s):
-        sv.write(s)
-        return render(np.zeros(6))
-
-    np.testing.assert_array_equal(depth_at(s0), base)
-    sens = np.zeros_like(base)
-    for k in range(len(s0)):
-        dd = []
-        for sign in (1.0, -1.0):
-            s = s0.copy()
-            s[k] += sign * SCALE * H_FD
-            dd.append(depth_at(s))
-        dp, dm = dd
-        keep &= smooth(dp, dm, base, 0.03)
-        with np.errstate(invalid="ignore"):
-            sens = np.maximum(sens, np.where(keep, np.abs(dp - dm), 0.0))
-    sv.write(s0)
-    moved = np.flatnonzero(keep.reshape(-1) & (sens.reshape(-1) > 2e-6))
-    still = np.flatnonzero(keep.reshape(-1) & (sens.reshape(-1) == 0))
-    assert len(moved) >= 4 and len(still) >= 12, (len(moved), len(still))
-    pix = torch.from_numpy(np.concatenate([rng.choice(moved, min(12, len(moved)), replace=False),
-                                           rng.choice(still, 12, replace=False)])).cuda()
-    s0_t = torch.tensor(s0, dtype=torch.float64)
-
-    def f(xi, z):
-        d, _ = RaycastPoseSdf.apply(xi, s0_t + SCALE * z, sv, T0)
-        return d.reshape(-1)[pix].double().cpu()
-
-    xi = torch.zeros(6, dtype=torch.float64, requires_grad=True)
-    z = torch.zeros(len(s0), dtype=torch.float64, requires_grad=True)
-    try:
-        ok = torch.autograd.gradcheck(f, (xi, z), eps=H_FD, atol=1e-2, rtol=3e-2, nondet_tol=1e-6)
-    finally:
-        sv.write(s0)
-    assert ok
-    # the sdf gradient reaches the moved pixels
-    d, _ = RaycastPoseSdf.apply(xi, s0_t + SCALE * z, sv, T0)
-    d.reshape(-1)[pix[:4]].sum().backward()
-    sv.write(s0)
-    assert np.abs(z.grad.numpy()).max() > 1e-3
+    check_pose_sdf(v, wl.pose(34), block_grad, "cuda")
