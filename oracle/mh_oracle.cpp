@@ -27,9 +27,10 @@
 //     (the reference relies on __syncthreads across CTAs, recycle.cu:94-113);
 //   * deleting a hash entry never fails (the reference's FreeEntry gives up
 //     when the bucket mutex is still held, core/hash_table.h:199-244);
-//   * FP32 mode uses the algebraically equal, well-conditioned form of the
-//     PSDF variance update (update_bayesian.cu:179-181); FP64 mode uses the
-//     reference's form.
+//   * FP32 mode uses algebraically equal, well-conditioned forms of the PSDF
+//     update (update_bayesian.cu:140-181: the variance without its
+//     cancellation, the Beta moments over one denominator, 4 divisions in
+//     all); FP64 mode uses the reference's form.
 #include <algorithm>
 #include <atomic>
 #include <cassert>
