@@ -11,7 +11,10 @@ failures surface through ``stats()['error']``.
 
 Arrays: host inputs are numpy arrays; device inputs/outputs are given as
 integer device pointers or objects with ``data_ptr()`` (e.g. torch CUDA
-tensors), which is how PyTorch serves as plumbing for device memory.
+tensors), which is how PyTorch serves as plumbing for device memory.  The C
+side trusts the pointers it gets, so the frame, raycast and gradient buffers
+given as arrays or tensors are checked here for size, float32 type, layout
+and device (ValueError); raw integer pointers are taken as given.
 """
 from __future__ import annotations
 
@@ -53,6 +56,41 @@ def _dev(x):
     if hasattr(x, "data_ptr"):
         return C.c_void_p(x.data_ptr())
     return C.c_void_p(int(x))
+
+
+def _check_tensor(x, n, what, cuda):
+    """A torch tensor handed to the library as a buffer of n float32 values:
+    the C side trusts the pointer, so size, type, layout and device are
+    checked here (raw integer pointers cannot be)."""
+    if str(x.dtype) != "torch.float32":
+        raise ValueError(f"{what}: expected a float32 tensor, got {x.dtype}")
+    if x.numel() != n:
+        raise ValueError(f"{what}: expected {n} values, got {x.numel()}")
+    if not x.is_contiguous():
+        raise ValueError(f"{what}: tensor must be contiguous")
+    if bool(x.is_cuda) != cuda:
+        raise ValueError(f"{what}: expected a {'CUDA' if cuda else 'host'} tensor")
+
+
+def _dev_buf(x, n, what):
+    """Device buffer of n float32 values: a CUDA tensor (checked) or an
+    integer device pointer (taken as given)."""
+    if x is not None and hasattr(x, "data_ptr"):
+        _check_tensor(x, n, what, cuda=True)
+    return _dev(x)
+
+
+def _host_out(x, n, what):
+    """Host output buffer of n float32 values: a numpy array or a CPU tensor."""
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        _check_tensor(x, n, what, cuda=False)
+        return C.c_void_p(x.data_ptr())
+    if not isinstance(x, np.ndarray) or x.dtype != np.float32 or x.size != n or not x.flags.c_contiguous \
+            or not x.flags.writeable:
+        raise ValueError(f"{what}: expected a writable C-contiguous float32 array of {n} values")
+    return x.ctypes.data_as(C.c_void_p)
 
 
 def default_params() -> MhParams:
@@ -103,14 +141,17 @@ class Volume:
         """Sensor::Process + Sensor::set_transform."""
         m = _f32(wTc).reshape(16)
         if on_device:
-            self._c("mh_frame_set", _dev(depth), 1, _ptr(m), self.stream)
+            self._c("mh_frame_set", _dev_buf(depth, self.W * self.H, "depth"), 1, _ptr(m), self.stream)
         else:
             d = _f32(depth).reshape(-1)
-            assert d.size == self.W * self.H
+            if d.size != self.W * self.H:
+                raise ValueError(f"depth: expected {self.W * self.H} values, got {d.size}")
             self._c("mh_frame_set", d.ctypes.data_as(C.c_void_p), 0, _ptr(m), self.stream)
 
     def set_frame_u16(self, depth, wTc):
         d = np.ascontiguousarray(depth, np.uint16).reshape(-1)
+        if d.size != self.W * self.H:
+            raise ValueError(f"depth: expected {self.W * self.H} values, got {d.size}")
         m = _f32(wTc).reshape(16)
         self._c("mh_frame_set_u16", d.ctypes.data_as(C.c_void_p), 0, _ptr(m), self.stream)
 
@@ -163,7 +204,9 @@ class Volume:
             self._c("mh_raycast", _ptr(m), d.ctypes.data_as(C.c_void_p), v.ctypes.data_as(C.c_void_p),
                     n.ctypes.data_as(C.c_void_p), 0, self.stream)
             return d.reshape(self.RH, self.RW), v.reshape(self.RH, self.RW, 4), n.reshape(self.RH, self.RW, 4)
-        self._c("mh_raycast", _ptr(m), _dev(depth_out), _dev(vertex_out), _dev(normal_out), 1, self.stream)
+        n = self.RW * self.RH
+        self._c("mh_raycast", _ptr(m), _dev_buf(depth_out, n, "depth_out"), _dev_buf(vertex_out, 4 * n, "vertex_out"),
+                _dev_buf(normal_out, 4 * n, "normal_out"), 1, self.stream)
         return None
 
     def raycast_footprint(self, cTw) -> int:
@@ -227,7 +270,10 @@ class Volume:
         floats, laid out like the voxel storage) receives dL/dsdf added in."""
         m = _f32(cTw).reshape(16)
         xi = (C.c_double * 6)()
-        self._c("mh_raycast_backward", _ptr(m), _dev(dL_ddepth), _dev(dL_dnormal), _dev(grad_sdf), xi, self.stream)
+        n = self.RW * self.RH
+        self._c("mh_raycast_backward", _ptr(m), _dev_buf(dL_ddepth, n, "dL_ddepth"),
+                _dev_buf(dL_dnormal, 4 * n, "dL_dnormal"),
+                _dev_buf(grad_sdf, self.params.value_capacity * 512, "grad_sdf"), xi, self.stream)
         return np.array(list(xi))
 
     def normal_equations(self, cTw, obs_depth=None, max_residual: float = 0.1):
@@ -285,16 +331,21 @@ class Volume:
                         ray_depth=None, ray_vertex=None, ray_normal=None, outputs_on_device: bool = False):
         """One MainEngine frame: Mapping, Meshing, raycast, Recycle."""
         m = _f32(wTc).reshape(16)
+        npx, nray = self.W * self.H, self.RW * self.RH
         if on_device:
-            dp = _dev(depth)
+            dp = _dev_buf(depth, npx, "depth")
         elif hasattr(depth, "data_ptr"):
+            _check_tensor(depth, npx, "depth", cuda=False)
             dp = _hptr(depth)
         else:
             d = _f32(depth).reshape(-1)
+            if d.size != npx:
+                raise ValueError(f"depth: expected {npx} values, got {d.size}")
             dp = d.ctypes.data_as(C.c_void_p)
-        conv = _dev if outputs_on_device else _hptr
+        conv = _dev_buf if outputs_on_device else _host_out
         self._c("mh_integrate_frame", dp, 1 if on_device else 0, _ptr(m), int(tv_iterations), C.c_float(tv_lambda),
-                conv(ray_depth), conv(ray_vertex), conv(ray_normal), 1 if outputs_on_device else 0, self.stream)
+                conv(ray_depth, nray, "ray_depth"), conv(ray_vertex, 4 * nray, "ray_vertex"),
+                conv(ray_normal, 4 * nray, "ray_normal"), 1 if outputs_on_device else 0, self.stream)
 
     # ---------------------------------------------------------- introspection
     def stats(self) -> dict:
