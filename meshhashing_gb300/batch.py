@@ -13,6 +13,7 @@ import numpy as np
 
 from . import _lib
 from ._abi import MhBatchTuning
+from .volume import _check_tensor
 
 RAY_TILE_SHAPES = ((16, 8), (8, 8), (32, 4))
 INTEGRATE_CTA_CAPS = (4, 8, 16)
@@ -46,17 +47,28 @@ class Batch:
              tv_lambda: float = 0.1, use_graph: bool = False, stream: int = 0):
         """One frame for every active scene.  depths: per scene an (H, W) float32
         array (host) or a CUDA tensor / device pointer (on_device); inactive
-        scenes may pass None.  poses: per scene a 4x4 camera-to-world matrix."""
+        scenes may pass None.  poses: per scene a 4x4 camera-to-world matrix.
+        Arrays and tensors are checked against each scene's frame size
+        (ValueError); raw device pointers are taken as given."""
         n = len(self.volumes)
+        if len(depths) != n or len(poses) != n:
+            raise ValueError(f"depths and poses need one entry per scene ({n})")
+        if active is not None and len(active) != n:
+            raise ValueError(f"active needs one entry per scene ({n})")
         keep = []
         ptrs = (C.c_void_p * n)()
         for i, d in enumerate(depths):
+            npx = self.volumes[i].W * self.volumes[i].H
             if d is None:
                 ptrs[i] = None
             elif on_device:
+                if hasattr(d, "data_ptr"):
+                    _check_tensor(d, npx, f"depths[{i}]", cuda=True)
                 ptrs[i] = d.data_ptr() if hasattr(d, "data_ptr") else int(d)
             else:
                 a = np.ascontiguousarray(d, np.float32)
+                if a.size != npx:
+                    raise ValueError(f"depths[{i}]: expected {npx} values, got {a.size}")
                 keep.append(a)
                 ptrs[i] = a.ctypes.data
         P = np.zeros((n, 16), np.float32)

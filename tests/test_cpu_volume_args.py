@@ -1,5 +1,5 @@
-"""Argument checks of the Python host layer (meshhashing_gb300.Volume), on the
-CPU: the C library trusts the pointers it is given, so frame, raycast and
+"""Argument checks of the Python host layer (meshhashing_gb300.Volume and
+Batch), on the CPU: the C library trusts the pointers it is given, so frame, raycast and
 gradient buffers passed as arrays or tensors must be refused with ValueError
 when their size, type, layout or device is wrong, before any call reaches the
 library.  The library is replaced by a recorder, so no GPU is needed."""
@@ -108,3 +108,26 @@ def test_raycast_and_backward_buffers():
     with pytest.raises(ValueError):
         v.raycast_backward(cTw, FakeTensor(W * H, dtype="torch.float16"), None, None)
     assert v.L.calls == ["mh_raycast", "mh_raycast_backward"]
+
+
+def test_batch_step_inputs():
+    from meshhashing_gb300.batch import Batch
+    b = object.__new__(Batch)
+    b.L = Recorder()
+    b.h = C.c_void_p()
+    b.volumes = [SimpleNamespace(W=W, H=H), SimpleNamespace(W=2 * W, H=2 * H)]
+    d0, d1 = np.zeros((H, W), np.float32), np.zeros((2 * H, 2 * W), np.float32)
+    b.step([d0, d1], [T, T])
+    b.step([d0, None], [T, None], active=[1, 0])
+    with pytest.raises(ValueError):
+        b.step([d1, d0], [T, T])                            # sizes swapped
+    with pytest.raises(ValueError):
+        b.step([d0], [T])                                   # one entry per scene
+    with pytest.raises(ValueError):
+        b.step([d0, d1], [T, T], active=[1])
+    b.step([FakeTensor(W * H), FakeTensor(4 * W * H)], [T, T], on_device=True)
+    with pytest.raises(ValueError):
+        b.step([FakeTensor(W * H), FakeTensor(W * H)], [T, T], on_device=True)
+    with pytest.raises(ValueError):
+        b.step([FakeTensor(W * H, cuda=False), None], [T, None], on_device=True)
+    assert b.L.calls == ["mh_batch_step"] * 3
