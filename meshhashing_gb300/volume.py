@@ -284,8 +284,8 @@ class Volume:
         b = (C.c_double * 6)()
         cost = C.c_double()
         cnt = C.c_int32()
-        self._c("mh_raycast_normal_equations", _ptr(m), _dev(obs_depth), C.c_float(max_residual), A, b,
-                C.byref(cost), C.byref(cnt), self.stream)
+        self._c("mh_raycast_normal_equations", _ptr(m), _dev_buf(obs_depth, self.RW * self.RH, "obs_depth"),
+                C.c_float(max_residual), A, b, C.byref(cost), C.byref(cnt), self.stream)
         return np.array(list(A)).reshape(6, 6), np.array(list(b)), cost.value, cnt.value
 
     def refine_pose(self, wTc, iterations: int = 10, obs_depth=None, max_residual: float = 0.1):
@@ -293,8 +293,8 @@ class Volume:
         m = np.ascontiguousarray(np.asarray(wTc, np.float32).reshape(16))
         cost = C.c_double()
         cnt = C.c_int32()
-        self._c("mh_refine_pose", _dev(obs_depth), _ptr(m), int(iterations), C.c_float(max_residual), C.byref(cost),
-                C.byref(cnt), self.stream)
+        self._c("mh_refine_pose", _dev_buf(obs_depth, self.RW * self.RH, "obs_depth"), _ptr(m), int(iterations),
+                C.c_float(max_residual), C.byref(cost), C.byref(cnt), self.stream)
         return m.reshape(4, 4), cost.value, cnt.value
 
     def point_to_psdf(self, wTc, reference_jacobian: bool = False):
@@ -320,11 +320,12 @@ class Volume:
         """(positions, rows) of a device per-voxel field laid out like the
         voxel storage (e.g. the grad_sdf of raycast_backward)."""
         n = C.c_int32()
-        self._c("mh_dump_block_field", _dev(field), 0, None, None, C.byref(n))
+        fp = _dev_buf(field, self.params.value_capacity * 512, "field")
+        self._c("mh_dump_block_field", fp, 0, None, None, C.byref(n))
         cnt = n.value
         pos = np.zeros((max(cnt, 1), 3), np.int32)
         out = np.zeros((max(cnt, 1), 512), np.float32)
-        self._c("mh_dump_block_field", _dev(field), cnt, _ptr(pos, C.c_int32), _ptr(out), C.byref(n))
+        self._c("mh_dump_block_field", fp, cnt, _ptr(pos, C.c_int32), _ptr(out), C.byref(n))
         return pos[:cnt], out[:cnt]
 
     def integrate_frame(self, depth, wTc, on_device: bool = False, tv_iterations: int = 0, tv_lambda: float = 0.1,

@@ -131,3 +131,16 @@ def test_batch_step_inputs():
     with pytest.raises(ValueError):
         b.step([FakeTensor(W * H, cuda=False), None], [T, None], on_device=True)
     assert b.L.calls == ["mh_batch_step"] * 3
+
+
+def test_pose_and_field_buffers():
+    v = volume()
+    v.normal_equations(np.eye(4), FakeTensor(W * H))
+    v.refine_pose(np.eye(4), obs_depth=None)
+    with pytest.raises(ValueError):
+        v.refine_pose(np.eye(4), obs_depth=FakeTensor(W * H - 1))
+    v.dump_block_field(FakeTensor(16 * 512))
+    with pytest.raises(ValueError):
+        v.dump_block_field(FakeTensor(16 * 511))
+    assert v.L.calls == ["mh_raycast_normal_equations", "mh_refine_pose", "mh_dump_block_field",
+                         "mh_dump_block_field"]
