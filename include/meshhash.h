@@ -80,8 +80,11 @@ typedef struct mh_params {
   int32_t  compat_arithmetic;     /* 1: evaluate the reference's single-precision
                                      formulas as written (results bit-compatible
                                      with the reference's own kernels);
-                                     0: well-conditioned equivalent forms of the
-                                     two that cancel (default) */
+                                     0 (default): algebraically equal forms
+                                     without the reference's cancellations --
+                                     the PSDF update with 4 divisions (variance
+                                     and Beta moments restated), the simple
+                                     update's weight as (dmax - d) / (dmax - dmin) */
 } mh_params;
 
 typedef struct mh_stats {
